@@ -1,0 +1,386 @@
+"""Benchmark of the FX correlator hot path (FxKernel::process) on GB300.
+
+Workload (default): 16 antennas x 2 pols, 2-bit real at 512 Msamples/s per pol
+(256 MHz), 1.0 s sub-integration, nchan 4096 (8192-point FFTs, 62500 FFTs),
+FP32 end to end, 136 baselines (autos included) x 4 products.
+Metric: input Gsamples/s = nant * 2 pols * nfft * F / seconds per sub-integration.
+
+value: device-resident inputs, one process() per step, CUDA events on the
+launching stream.  e2e: the same call through the C ABI with pinned HOST input
+buffers (host->device copy inside process()) plus the device->host read of the
+visibilities, every step.  Multi-GPU (torchrun): independent replicas, one
+sub-integration per rank per step, no collective on the data path.
+
+--impl reference times the CPU implementation of the path (the FP32 port of
+fxkernel in oracle/, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "c0": ("6 antennas, 2-bit real, 128 Ms/s per pol, 0.25 s, nchan 1024", "config0"),
+    "c1": ("16 antennas, 2-bit real, 512 Ms/s per pol, 1.0 s, nchan 4096", "config1"),
+    "c2": ("32 antennas, 2-bit real, 1024 Ms/s per pol, 0.5 s, nchan 8192, rho 0.01, tone", "config2"),
+}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world, backend):
+    import torch.distributed as dist
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group(backend=backend)
+    return dist
+
+
+def reduce_max(x: float, world: int, device=None) -> float:
+    """Max over ranks (timing rule: the slowest replica sets the job time)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int, path: str):
+        self.path = path
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        load = [s for s in sm if mx and s > 0.3 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def workload(name):
+    from gcorr_gb300 import synth
+    return getattr(synth, CONFIGS[name][1])()
+
+
+# ---------------------------------------------------------------- CPU side
+def cpu_port_run(w, nfft_sample: int, nthreads: int, seed_inputs=None):
+    """Times the FP32 port of fxkernel (oracle) on nfft_sample FFTs of workload w."""
+    import dataclasses
+    import numpy as np
+    from gcorr_gb300 import synth
+    from oracle import oracle as O
+    ws = dataclasses.replace(w, nfft=nfft_sample)
+    if seed_inputs is None:
+        d = synth.random_bytes(ws)
+        seed_inputs = ([x.numpy() for x in d["inputs"]], d["poly"], d["fso"])
+    inputs, poly, fso = seed_inputs
+    cfg = O.config_from_workload(ws, O.ROT_FXKERNEL if int(round(w.nchan ** 0.5)) ** 2 == w.nchan else O.ROT_EXACT,
+                                 True)
+    t0 = time.perf_counter()
+    O.port_process(cfg, inputs, poly, fso, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    samples = ws.nant * 2 * ws.nfft * ws.fft_len
+    return samples / dt, dt, seed_inputs
+
+
+def cpu_sample(w, budget_s: float = 12.0):
+    """Picks a bounded FFT sample taking about budget_s of CPU work on all threads."""
+    nthreads = os.cpu_count() or 1
+    n = max(nthreads, 1)
+    rate, dt, _ = cpu_port_run(w, n, nthreads)
+    per_fft = dt / n
+    n2 = int(max(n, min(w.nfft, budget_s / max(per_fft, 1e-6))))
+    n2 -= n2 % nthreads if n2 > nthreads else 0
+    rate, dt, _ = cpu_port_run(w, n2, nthreads)
+    return {"value": rate / 1e9, "unit": "input Gsamples/s", "cores": nthreads, "kind": "port",
+            "sample": f"{n2} of {w.nfft} FFTs of the same workload (random 2-bit bytes, fxkernel-rotator FP32 port, "
+                      f"{nthreads} threads), {dt:.1f} s", "seconds": dt}
+
+
+def run_reference_arm(args):
+    rank, world, local = dist_env()
+    if world > 1:
+        init_dist(world, "gloo")
+        if rank != 0:
+            barrier(world)
+            return
+    w = workload(args.config)
+    nthreads = os.cpu_count() or 1
+    # one step = the port on a bounded FFT sample (about args.ref_step_s of CPU time)
+    rate, dt, seed = cpu_port_run(w, nthreads, nthreads)
+    n = int(max(nthreads, min(w.nfft, args.ref_step_s / max(dt / nthreads, 1e-6))))
+    n -= n % nthreads if n > nthreads else 0
+    rate, dt, seed = cpu_port_run(w, n, nthreads)
+    for _ in range(args.warmup):
+        cpu_port_run(w, n, nthreads, seed)
+    times = []
+    for _ in range(args.steps):
+        r, dt, _ = cpu_port_run(w, n, nthreads, seed)
+        times.append(dt)
+    tot = sum(times)
+    samples = w.nant * 2 * n * w.fft_len * args.steps
+    val = samples / tot / 1e9
+    line = {"impl": "reference", "metric": "input Gsamples/s", "value": val, "unit": "input Gsamples/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": CONFIGS[args.config][0], "sample_ffts_per_step": n, "nfft": w.nfft,
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": val, "unit": "input Gsamples/s", "cores": nthreads, "kind": "port",
+                             "sample": f"{n} of {w.nfft} FFTs per step, FP32 port of fxkernel (oracle/fxoracle.c), "
+                                       f"{nthreads} threads (IPP unavailable)"},
+            "e2e": {"value": val, "unit": "input Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        barrier(world)
+
+
+# ---------------------------------------------------------------- GPU side
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gxcorr", choices=["gxcorr", "reference"])
+    ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16"])
+    ap.add_argument("--x-engine", default="auto", choices=["auto", "cuda_core", "tensor"])
+    ap.add_argument("--fft-block", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--ref-step-s", type=float, default=6.0)
+    ap.add_argument("--out-dir", default=os.path.join(ROOT, "gpurun_out"))
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import numpy as np
+    import torch
+    import gcorr_gb300 as G
+    from gcorr_gb300 import synth
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = init_dist(world, "nccl")
+    dev = torch.device("cuda", local)
+    w = synth.Workload(**{**workload(args.config).__dict__, "seed": 1234 + 7919 * rank})
+    tg = time.perf_counter()
+    d = synth.generate(w, device=dev)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - tg
+    inputs_dev = d["inputs"]
+    stream = torch.cuda.Stream(device=dev)
+
+    fx = G.FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=args.precision,
+                    rotator="exact", autos=True, x_engine=args.x_engine, fft_block=args.fft_block, device=local)
+    fx.setInputData(inputs_dev)
+    fx.setDelays(d["poly"], d["fso"])
+    sptr = stream.cuda_stream
+
+    def step():
+        fx.process(stream=sptr, sync=False)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    launches_per_step = fx.launches
+
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    os.makedirs(args.out_dir, exist_ok=True)
+    clk = ClockSampler(local, os.path.join(args.out_dir, f"clocks_r{rank}.csv"))
+    barrier(world)
+    torch.cuda.synchronize()
+    with clk:
+        time.sleep(0.3)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms_max = reduce_max(ms, world, dev)
+    clocks = clk.summary()
+
+    # stage split (separate, untimed run with per-block events)
+    fx.enable_stage_timing(True)
+    step()
+    f_ms, x_ms, tot_ms = fx.stage_times()
+    fx.enable_stage_timing(False)
+    vis0 = fx.visibilities()
+
+    samples = w.nant * 2 * w.nfft * w.fft_len
+    value = samples * world / (ms_max / 1e3) / 1e9
+
+    # e2e: pinned host inputs through the C ABI, H2D inside process(), D2H of the visibilities
+    e2e = None
+    if not args.no_e2e:
+        host = [x.cpu().pin_memory() for x in inputs_dev]
+        fxh = G.FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=args.precision,
+                         rotator="exact", autos=True, x_engine=args.x_engine, fft_block=args.fft_block, device=local)
+        fxh.setInputData(host)
+        fxh.setDelays(d["poly"], d["fso"])
+        out = torch.empty((fxh.nbaselines, 4, w.nchan), dtype=torch.complex64).pin_memory()
+        for _ in range(args.warmup):
+            fxh.process(stream=sptr, sync=False)
+            L_ = G.lib()
+            import ctypes as C
+            G._lib.check(L_.gxc_get_visibilities(fxh._h, C.c_void_p(out.data_ptr())), fxh._h, "get")
+        torch.cuda.synchronize()
+        barrier(world)
+        import ctypes as C
+        t0 = time.perf_counter()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fxh.process(stream=sptr, sync=False)
+            G._lib.check(G.lib().gxc_get_visibilities(fxh._h, C.c_void_p(out.data_ptr())), fxh._h, "get")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) / args.steps * 1e3
+        ems = max(e0.elapsed_time(e1) / args.steps, wall)
+        ems = reduce_max(ems, world, dev)
+        h2d = sum(int(x.numel()) for x in host)
+        d2h = int(out.numel()) * 8
+        vis_h = out.numpy()
+        e2e = {"value": samples * world / (ems / 1e3) / 1e9, "unit": "input Gsamples/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ems,
+               "matches_device_run": bool(np.allclose(vis_h, vis0, rtol=1e-5, atol=1e-6))}
+        fxh.close()
+
+    # roofline of the dominant kernel
+    pk = peaks()
+    esz = 8 if args.precision == "fp32" else 4
+    in_bytes = w.bytes_per_antenna * w.nant
+    chan_bytes = w.nant * 2 * w.nfft * w.nchan * esz
+    nprod = 4 * w.nant * (w.nant + 1) // 2
+    xflops = 8.0 * nprod * w.nchan * w.nfft
+    fftflops = 5.0 * w.fft_len * np.log2(w.fft_len) * 2 * w.nant * w.nfft
+    f_gbs = (in_bytes + chan_bytes) / (f_ms / 1e3) / 1e9
+    x_gbs = chan_bytes / (x_ms / 1e3) / 1e9
+    if f_ms >= x_ms:
+        roof = {"kernel": "fstage_kernel (unpack+rotate+FFT+frac-delay)", "bound": "hbm", "achieved": f_gbs,
+                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": f_gbs / pk["hbm_gbs"], "traffic": None,
+                "algorithmic_bytes_per_step": in_bytes + chan_bytes, "fft_tflops": fftflops / (f_ms / 1e3) / 1e12,
+                "peak_source": pk["source"]}
+    else:
+        roof = {"kernel": "xstage", "bound": "hbm", "achieved": x_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": x_gbs / pk["hbm_gbs"], "traffic": None, "algorithmic_bytes_per_step": chan_bytes,
+                "x_tflops": xflops / (x_ms / 1e3) / 1e12, "peak_source": pk["source"]}
+    tfile = os.path.join(ROOT, "profiles", f"traffic_{args.config}_{args.precision}.json")
+    if os.path.exists(tfile):
+        roof["traffic"] = json.load(open(tfile)).get(roof["kernel"].split()[0])
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_sample(w)
+
+    if rank == 0:
+        line = {
+            "metric": "input Gsamples/s", "value": value, "unit": "input Gsamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f16",
+            "data": "synthetic",
+            "config": {"workload": CONFIGS[args.config][0], "nant": w.nant, "nchan": w.nchan, "nfft": w.nfft,
+                       "fft_len": w.fft_len, "nbit": w.nbit, "precision": args.precision,
+                       "x_engine": args.x_engine, "fft_block": fx.fft_block, "autos": True,
+                       "parallelism": f"replicas x{world}",
+                       "l2": f"inputs larger than L2 ({in_bytes / 1e9:.1f} GB packed, "
+                             f"{chan_bytes / 1e9:.1f} GB channelised per step)"},
+            "stage_ms": {"f": f_ms, "x": x_ms, "total": tot_ms},
+            "x_tflops": xflops / (x_ms / 1e3) / 1e12,
+            "gpu_launches": launches_per_step * args.steps,
+            "roofline": roof,
+            "clocks": clocks,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "generator_s": gen_s,
+        }
+        print(json.dumps(line), flush=True)
+    fx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

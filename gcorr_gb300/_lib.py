@@ -1,0 +1,113 @@
+"""ctypes declarations for libgxcorr.so (the C ABI in include/gxc.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgxcorr.so")
+
+GXC_OK = 0
+GXC_ERR_INVALID_ARGUMENT = 1
+GXC_ERR_UNSUPPORTED = 2
+GXC_ERR_CUDA = 3
+GXC_ERR_OUT_OF_MEMORY = 4
+GXC_ERR_STATE = 5
+GXC_ERR_TIMEOUT = 6
+GXC_PRECISION_FP32, GXC_PRECISION_FP16, GXC_PRECISION_FP8 = 0, 1, 2
+GXC_ROTATOR_EXACT, GXC_ROTATOR_FXKERNEL = 0, 1
+GXC_XENGINE_AUTO, GXC_XENGINE_CUDA_CORE, GXC_XENGINE_TENSOR = 0, 1, 2
+_STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "out of memory",
+           5: "bad call order", 6: "device wait timed out"}
+
+# every function include/gxc.h declares (the CPU tests check the export list against the header)
+EXPORTS = [
+    "gxc_config_init", "gxc_validate_config", "gxc_input_bytes_per_antenna", "gxc_num_baselines",
+    "gxc_status_string", "gxc_create", "gxc_destroy", "gxc_set_input", "gxc_set_delays", "gxc_process",
+    "gxc_sync", "gxc_accumulate", "gxc_get_visibilities", "gxc_device_visibilities", "gxc_get_baseline_counts",
+    "gxc_get_valid_flags", "gxc_last_error", "gxc_last_launch_count", "gxc_fft_block", "gxc_enable_stage_timing",
+    "gxc_stage_times",
+]
+
+
+class GxcConfig(C.Structure):
+    _fields_ = [("nant", C.c_int), ("nchan", C.c_int), ("nfft", C.c_int), ("nbit", C.c_int),
+                ("is_complex", C.c_int), ("lo_hz", C.c_double), ("bw_hz", C.c_double), ("precision", C.c_int),
+                ("rotator", C.c_int), ("autos", C.c_int), ("x_engine", C.c_int), ("fft_block", C.c_int),
+                ("device", C.c_int)]
+
+
+class GxcError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(msg)
+        self.status = status
+
+
+_lib = None
+
+
+def status_name(st: int) -> str:
+    return _STATUS.get(int(st), f"status {st}")
+
+
+def lib():
+    """Load libgxcorr.so; raises if it has not been built (no fallback path exists)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with gcorr_gb300.build()")
+        l = C.CDLL(LIB_PATH)
+        P, V = C.POINTER, C.c_void_p
+        l.gxc_config_init.argtypes = [P(GxcConfig)]
+        l.gxc_config_init.restype = None
+        l.gxc_validate_config.argtypes = [P(GxcConfig)]
+        l.gxc_validate_config.restype = C.c_int
+        l.gxc_input_bytes_per_antenna.argtypes = [P(GxcConfig)]
+        l.gxc_input_bytes_per_antenna.restype = C.c_size_t
+        l.gxc_num_baselines.argtypes = [P(GxcConfig)]
+        l.gxc_num_baselines.restype = C.c_int
+        l.gxc_status_string.argtypes = [C.c_int]
+        l.gxc_status_string.restype = C.c_char_p
+        l.gxc_create.argtypes = [P(GxcConfig), P(V)]
+        l.gxc_create.restype = C.c_int
+        l.gxc_destroy.argtypes = [V]
+        l.gxc_destroy.restype = C.c_int
+        l.gxc_set_input.argtypes = [V, V, C.c_size_t]
+        l.gxc_set_input.restype = C.c_int
+        l.gxc_set_delays.argtypes = [V, V, V]
+        l.gxc_set_delays.restype = C.c_int
+        l.gxc_process.argtypes = [V, V]
+        l.gxc_process.restype = C.c_int
+        l.gxc_sync.argtypes = [V]
+        l.gxc_sync.restype = C.c_int
+        l.gxc_accumulate.argtypes = [V, V]
+        l.gxc_accumulate.restype = C.c_int
+        l.gxc_get_visibilities.argtypes = [V, V]
+        l.gxc_get_visibilities.restype = C.c_int
+        l.gxc_device_visibilities.argtypes = [V]
+        l.gxc_device_visibilities.restype = V
+        l.gxc_get_baseline_counts.argtypes = [V, V]
+        l.gxc_get_baseline_counts.restype = C.c_int
+        l.gxc_get_valid_flags.argtypes = [V, V]
+        l.gxc_get_valid_flags.restype = C.c_int
+        l.gxc_last_error.argtypes = [V]
+        l.gxc_last_error.restype = C.c_char_p
+        l.gxc_last_launch_count.argtypes = [V]
+        l.gxc_last_launch_count.restype = C.c_int
+        l.gxc_fft_block.argtypes = [V]
+        l.gxc_fft_block.restype = C.c_int
+        l.gxc_enable_stage_timing.argtypes = [V, C.c_int]
+        l.gxc_enable_stage_timing.restype = C.c_int
+        l.gxc_stage_times.argtypes = [V, V, V, V]
+        l.gxc_stage_times.restype = C.c_int
+        _lib = l
+    return _lib
+
+
+def check(st: int, handle, what: str):
+    if st != GXC_OK:
+        msg = ""
+        if handle is not None:
+            m = lib().gxc_last_error(handle)
+            msg = m.decode() if m else ""
+        raise GxcError(st, f"{what}: {status_name(st)}" + (f": {msg}" if msg else ""))

@@ -1,0 +1,475 @@
+// F-stage of the FX correlator: per-(antenna, FFT) geometry, validity counts,
+// and the fused channelising kernel (unpack -> fringe rotation -> FFT ->
+// fractional-sample-delay correction -> cast -> write in the X-stage layout).
+//
+// Reference path restated: fxkernel/src/fxkernel.cpp:276-325 (station loop of
+// process()), :425-440 getStationDelay, :443-487 unpack, :498-567 fringerotate,
+// :569-580 dofft, :595-634 fracSampleCorrect.
+#include <math.h>
+#include <stdlib.h>
+#include <vector>
+
+#include "gxc_internal.h"
+
+namespace gxc {
+
+// ----------------------------------------------------------------- geometry
+// One thread per (antenna, FFT).  FP64 with explicit round-to-nearest
+// operations so the integer/fractional split matches the CPU reference bit
+// for bit (no FMA contraction): fxkernel.cpp:432-439 and :289-309.
+__global__ void geometry_kernel(Job job) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long total = (long long)job.nant * job.nfft;
+  if (idx >= total) return;
+  const int ant = (int)(idx / job.nfft);
+  const int i = (int)(idx % job.nfft);
+  const double *p = job.poly + 3 * ant;
+  const double fso = job.fso[ant];
+  const double fi = (double)i, fh = fi + 0.5, f1 = fi + 1.0;
+  const double d0 = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(p[0], fi), fi), __dmul_rn(p[1], fi)), p[2]);
+  const double d1 = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(p[0], fh), fh), __dmul_rn(p[1], fh)), p[2]);
+  const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(p[0], f1), f1), __dmul_rn(p[1], f1)), p[2]);
+  const double a = __dsub_rn(d2, d0);
+  const double b = __dadd_rn(d0, __ddiv_rn(__dsub_rn(d1, __dadd_rn(__dmul_rn(a, 0.5), d0)), 3.0));
+  const double mean = __dadd_rn(__dmul_rn(a, 0.5), b);
+  const double ndf = __ddiv_rn(__dsub_rn(mean, fso), job.Ts);
+  Geom g;
+  g.a = a;
+  g.b = b;
+  g.frac = 0.0;
+  g.offset = 0;
+  g.valid = 0;
+  if (fabs(ndf) < 1.0e9) {  // false for NaN/Inf: flagged instead of undefined int()
+    const int nd = __double2int_rz(__dadd_rn(ndf, 0.5));
+    double frac = -__dmul_rn(__dsub_rn(ndf, (double)nd), job.Ts);
+    long long off = (long long)i * job.F - nd;
+    if (off == -1) { off++; frac = __dadd_rn(frac, job.Ts); }
+    if (off == job.maxoffset + 1) { off--; frac = __dsub_rn(frac, job.Ts); }
+    g.frac = frac;
+    if (off >= 0 && off <= job.maxoffset) {
+      g.offset = (int)off;
+      g.valid = 1;
+    }
+  }
+  job.geom[idx] = g;
+}
+
+cudaError_t launch_geometry(const Job &job, cudaStream_t s) {
+  const long long total = (long long)job.nant * job.nfft;
+  const int threads = 256;
+  const long long blocks = (total + threads - 1) / threads;
+  geometry_kernel<<<(unsigned)blocks, threads, 0, s>>>(job);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------- counts
+// counts[bl] = number of FFTs where both antennas are valid (fxkernel.cpp:352),
+// plus the antValid flags exported as uint8 [nant][nfft].
+__global__ void counts_kernel(const Geom *__restrict__ geom, int nant, int nfft, int autos, int32_t *counts,
+                              uint8_t *valid_flags) {
+  const int bl = blockIdx.x;
+  const int ncross = nant * (nant - 1) / 2;
+  int j, k;
+  if (bl >= ncross) {
+    j = k = bl - ncross;
+  } else {  // invert the fxkernel baseline order
+    j = 0;
+    int rem = bl;
+    while (rem >= nant - 1 - j) { rem -= nant - 1 - j; j++; }
+    k = j + 1 + rem;
+  }
+  int c = 0;
+  for (int t = threadIdx.x; t < nfft; t += blockDim.x) {
+    const int vj = geom[(size_t)j * nfft + t].valid;
+    const int vk = geom[(size_t)k * nfft + t].valid;
+    c += (vj && vk) ? 1 : 0;
+    if (valid_flags && bl == 0) {
+      // block 0 also exports every antenna's flags
+      for (int a = 0; a < nant; a++) valid_flags[(size_t)a * nfft + t] = (uint8_t)geom[(size_t)a * nfft + t].valid;
+    }
+  }
+  __shared__ int red[32];
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int v = (threadIdx.x < (int)(blockDim.x >> 5)) ? red[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) counts[bl] = v;
+  }
+}
+
+cudaError_t launch_counts(const Job &job, int autos, int32_t *counts, uint8_t *valid_flags, cudaStream_t s) {
+  const int nbl = job.nant * (job.nant - 1) / 2 + (autos ? job.nant : 0);
+  if (nbl == 0) return cudaSuccess;
+  counts_kernel<<<nbl, 256, 0, s>>>(job.geom, job.nant, job.nfft, autos, counts, valid_flags);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------------- twiddles
+// tw[m] = exp(-2 pi i m / F), m < F, rounded once from double.
+cudaError_t make_twiddles(int F, float2 **out) {
+  std::vector<float2> h((size_t)F);
+  for (int m = 0; m < F; m++) {
+    const double ang = -2.0 * 3.14159265358979323846 * (double)m / (double)F;
+    h[(size_t)m] = make_float2((float)cos(ang), (float)sin(ang));
+  }
+  cudaError_t e = cudaMalloc((void **)out, sizeof(float2) * (size_t)F);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*out, h.data(), sizeof(float2) * (size_t)F, cudaMemcpyHostToDevice);
+}
+
+// ------------------------------------------------------------ FFT helpers
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// -i * a
+__device__ __forceinline__ float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }
+
+// Forward DFTs (W = exp(-2 pi i / R)) on registers, natural order in and out.
+__device__ __forceinline__ void dft2(float2 &a, float2 &b) {
+  const float2 t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+__device__ __forceinline__ void dft4(float2 &x0, float2 &x1, float2 &x2, float2 &x3) {
+  const float2 s02 = cadd(x0, x2), d02 = csub(x0, x2);
+  const float2 s13 = cadd(x1, x3), d13 = cmul_mi(csub(x1, x3));
+  x0 = cadd(s02, s13);
+  x2 = csub(s02, s13);
+  x1 = cadd(d02, d13);
+  x3 = csub(d02, d13);
+}
+template <int R> __device__ __forceinline__ void dft(float2 *u);
+template <> __device__ __forceinline__ void dft<2>(float2 *u) { dft2(u[0], u[1]); }
+template <> __device__ __forceinline__ void dft<4>(float2 *u) { dft4(u[0], u[1], u[2], u[3]); }
+// 8 = 4 (n1) x 2 (n2): n = 2 n1 + n2, k = k1 + 4 k2.
+template <> __device__ __forceinline__ void dft<8>(float2 *u) {
+  const float r = 0.70710678118654752440f;
+  dft4(u[0], u[2], u[4], u[6]);
+  dft4(u[1], u[3], u[5], u[7]);
+  // twiddle W8^(k1) on the n2 = 1 branch
+  u[3] = cmul(u[3], make_float2(r, -r));
+  u[5] = cmul_mi(u[5]);
+  u[7] = cmul(u[7], make_float2(-r, -r));
+  float2 y[8];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    float2 a = u[2 * k1], b = u[2 * k1 + 1];
+    dft2(a, b);
+    y[k1] = a;
+    y[k1 + 4] = b;
+  }
+#pragma unroll
+  for (int q = 0; q < 8; q++) u[q] = y[q];
+}
+// 16 = 4 (n1) x 4 (n2): n = 4 n1 + n2, k = k1 + 4 k2.
+template <> __device__ __forceinline__ void dft<16>(float2 *u) {
+  const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f, r = 0.70710678118654752440f;
+#pragma unroll
+  for (int n2 = 0; n2 < 4; n2++) dft4(u[n2], u[n2 + 4], u[n2 + 8], u[n2 + 12]);
+  // after this, u[n2 + 4 k1] holds Y[n2][k1]; twiddle by W16^(n2 k1)
+  u[5] = cmul(u[5], make_float2(c1, -s1));    // n2=1,k1=1: W^1
+  u[9] = cmul(u[9], make_float2(r, -r));      // n2=1,k1=2: W^2
+  u[13] = cmul(u[13], make_float2(s1, -c1));  // n2=1,k1=3: W^3
+  u[6] = cmul(u[6], make_float2(r, -r));      // n2=2,k1=1: W^2
+  u[10] = cmul_mi(u[10]);                     // n2=2,k1=2: W^4
+  u[14] = cmul(u[14], make_float2(-r, -r));   // n2=2,k1=3: W^6
+  u[7] = cmul(u[7], make_float2(s1, -c1));    // n2=3,k1=1: W^3
+  u[11] = cmul(u[11], make_float2(-r, -r));   // n2=3,k1=2: W^6
+  u[15] = cmul(u[15], make_float2(-c1, s1));  // n2=3,k1=3: W^9
+  float2 y[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    float2 a = u[4 * k1], b = u[4 * k1 + 1], c = u[4 * k1 + 2], d = u[4 * k1 + 3];
+    dft4(a, b, c, d);  // over n2
+    y[k1] = a;
+    y[k1 + 4] = b;
+    y[k1 + 8] = c;
+    y[k1 + 12] = d;
+  }
+#pragma unroll
+  for (int q = 0; q < 16; q++) u[q] = y[q];
+}
+
+// Shared-memory index padding: one float2 of padding per 16 keeps the
+// stride-R writes of the early Stockham passes free of bank conflicts.
+__device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
+
+__device__ __forceinline__ float level2bit(int code) {
+  // fxkernel.cpp:17-18: {-HiMag, -1, 1, HiMag}, HiMag = 3.3359
+  const float mag = (code == 0 || code == 3) ? 3.3359f : 1.0f;
+  return (code & 2) ? mag : -mag;
+}
+
+template <typename OutT> __device__ __forceinline__ OutT to_out(float2 v, float scale);
+template <> __device__ __forceinline__ float2 to_out<float2>(float2 v, float scale) {
+  return make_float2(v.x * scale, v.y * scale);
+}
+template <> __device__ __forceinline__ __half2 to_out<__half2>(float2 v, float scale) {
+  return __floats2half2_rn(v.x * scale, v.y * scale);
+}
+
+struct FParams {
+  Job job;
+  const float2 *tw;
+  int t0, T;
+  void *chan;
+  float out_scale;
+  int sub_shift, sub_mask;    // substride = 1 << sub_shift
+  int fsub_shift, fsub_mask;  // fsub = 1 << fsub_shift
+};
+
+// One Stockham pass (radix R, span P) reading smem, leaving results in u.
+template <int N, int R, int P>
+__device__ __forceinline__ void pass_load(const float2 *buf, const float2 *__restrict__ tw, float2 (&u)[16], int tid) {
+#pragma unroll
+  for (int q = 0; q < 16 / R; q++) {
+    const int iv = tid + q * (N / 16);
+    const int k = iv & (P - 1);
+#pragma unroll
+    for (int r = 0; r < R; r++) u[q * R + r] = buf[pidx(iv + r * (N / R))];
+    if (P > 1) {
+#pragma unroll
+      for (int r = 1; r < R; r++) u[q * R + r] = cmul(u[q * R + r], __ldg(&tw[r * k * (N / (P * R))]));
+    }
+    dft<R>(&u[q * R]);
+  }
+}
+
+template <int N, int R, int P>
+__device__ __forceinline__ void pass_store(float2 *buf, const float2 (&u)[16], int tid) {
+#pragma unroll
+  for (int q = 0; q < 16 / R; q++) {
+    const int iv = tid + q * (N / 16);
+    const int k = iv & (P - 1);
+    const int j = (iv - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) buf[pidx(j + r * P)] = u[q * R + r];
+  }
+}
+
+// Middle radix-16 passes, P = P0 .. N/256 (the last pass is handled by the caller).
+template <int N, int P>
+struct MidPasses {
+  __device__ __forceinline__ static void run(float2 *buf, const float2 *__restrict__ tw, float2 (&u)[16], int tid,
+                                             bool active) {
+    if constexpr (P * 16 < N) {
+      if (active) pass_load<N, 16, P>(buf, tw, u, tid);
+      __syncthreads();
+      if (active) pass_store<N, 16, P>(buf, u, tid);
+      __syncthreads();
+      MidPasses<N, P * 16>::run(buf, tw, u, tid, active);
+    }
+  }
+};
+
+template <int L>
+struct FftPlan {
+  static constexpr int N = 1 << L;
+  static constexpr int R0 = (L % 4) ? (1 << (L % 4)) : 16;
+  static constexpr int NV = N / 16;                 // threads doing FFT work
+  static constexpr int NT = NV < 32 ? 32 : NV;      // threads launched
+};
+
+template <int L, typename OutT, bool CPLX>
+__global__ void __launch_bounds__(FftPlan<L>::NT) fstage_kernel(FParams prm) {
+  using Plan = FftPlan<L>;
+  constexpr int N = Plan::N;
+  constexpr int R0 = Plan::R0;
+  constexpr int NV = Plan::NV;
+  constexpr int NT = Plan::NT;
+  const Job &job = prm.job;
+  extern __shared__ float2 smem[];
+  float2 *buf = smem;                          // N + N/16 (padded)
+  float2 *tsub = buf + N + N / 16;             // fringe rotator, fine part  [substride]
+  float2 *tstep = tsub + job.substride;        // fringe rotator, coarse part [stride]
+  float2 *fsubt = tstep + job.stride;          // frac-delay, fine part [fsub]
+  float2 *fstept = fsubt + job.fsub;           // frac-delay, coarse part [fstride]
+  __shared__ Geom g;
+  __shared__ float cst[4];
+
+  const int tl = blockIdx.x;
+  const int ant = blockIdx.y;
+  const int t = prm.t0 + tl;
+  const int tid = threadIdx.x;
+  const int nstreams = 2 * job.nant;
+  const int nchan = job.nchan;
+  OutT *chan = reinterpret_cast<OutT *>(prm.chan);
+
+  if (tid == 0) {
+    g = job.geom[(size_t)ant * job.nfft + t];
+    if (g.valid) {
+      // Per-FFT FP64 constants, reduced mod 1 turn before going to FP32
+      // (fxkernel.cpp:503-535): phase(n) = LO*(b + a*n/F) turns.
+      const int intdelay = __double2int_rz(g.b);
+      const double br = g.b - (double)intdelay;
+      double c0 = br * job.lo_hz;
+      if (job.fractional_lo) c0 += (job.lo_hz - trunc(job.lo_hz)) * (double)intdelay;
+      c0 -= floor(c0);
+      const double c1 = g.a * job.lo_hz / (double)job.F;  // turns per sample
+      // coarse step: the reference advances the step table by `stride` samples
+      // per entry (fxkernel.cpp:112) while applying it every `substride` samples;
+      // FXKERNEL mode keeps that, EXACT uses the true step.
+      const double stepmul = (job.rotator == GXC_ROTATOR_FXKERNEL) ? (double)job.stride : (double)job.substride;
+      cst[0] = (float)c0;
+      cst[1] = (float)c1;
+      cst[2] = (float)(c1 * stepmul);
+      // fractional-sample correction: exp(+2 pi i c bw/nchan frac) (fxkernel.cpp:171-175,600-630)
+      cst[3] = (float)(job.bw_hz / (double)nchan * g.frac);  // turns per channel
+    }
+  }
+  __syncthreads();
+
+  if (!g.valid) {
+    // flagged: the X-stage sums zeros, the baseline counts exclude this FFT
+    const OutT z = to_out<OutT>(make_float2(0.f, 0.f), 1.f);
+    for (int p = 0; p < 2; p++) {
+      const int s = 2 * ant + p;
+      for (int c = tid; c < nchan; c += NT) {
+        const size_t o = (((size_t)(c >> 4) * prm.T + tl) * nstreams + s) * CW + (c & 15);
+        chan[o] = z;
+      }
+    }
+    return;
+  }
+
+  {
+    const float c0 = cst[0], c1 = cst[1], cstep = cst[2], cf = cst[3];
+    for (int k = tid; k < job.substride; k += NT) {
+      float s, c;
+      sincospif(-2.0f * fmaf((float)k, c1, c0), &s, &c);
+      tsub[k] = make_float2(c, s);
+    }
+    for (int i = tid; i < job.stride; i += NT) {
+      float s, c;
+      sincospif(-2.0f * ((float)i * cstep), &s, &c);
+      tstep[i] = make_float2(c, s);
+    }
+    for (int k = tid; k < job.fsub; k += NT) {
+      float s, c;
+      sincospif(2.0f * ((float)k * cf), &s, &c);
+      fsubt[k] = make_float2(c, s);
+    }
+    for (int i = tid; i < job.fstride; i += NT) {
+      float s, c;
+      sincospif(2.0f * ((float)(i << prm.fsub_shift) * cf), &s, &c);
+      fstept[i] = make_float2(c, s);
+    }
+  }
+  __syncthreads();
+
+  const bool active = tid < NV;
+  const uint8_t *in = job.inputs[ant];
+  const long long off = g.offset;
+
+  for (int pol = 0; pol < 2; pol++) {
+    float2 u[16];
+    // ---- first pass: decode + rotate straight from the packed input
+    if (active) {
+#pragma unroll
+      for (int q = 0; q < 16 / R0; q++) {
+        const int iv = tid + q * NV;
+#pragma unroll
+        for (int r = 0; r < R0; r++) {
+          const int n = iv + r * (N / R0);
+          const float2 rot = cmul(tsub[n & prm.sub_mask], tstep[n >> prm.sub_shift]);
+          const long long m = off + n;
+          float2 x;
+          if constexpr (CPLX) {
+            // int8 (A.re, A.im, B.re, B.im) per time sample
+            const char2 v = __ldg(reinterpret_cast<const char2 *>(in + m * 4 + 2 * pol));
+            x = cmul(make_float2((float)v.x, (float)v.y), rot);
+          } else {
+            // 2-bit: byte m/2 holds A_m', B_m', A_m'+1, B_m'+1 (fxkernel.cpp:443-476)
+            const int byte = __ldg(in + (m >> 1));
+            const int code = (byte >> (2 * (2 * (int)(m & 1) + pol))) & 3;
+            const float v = level2bit(code);
+            x = make_float2(v * rot.x, v * rot.y);
+          }
+          u[q * R0 + r] = x;
+        }
+        dft<R0>(&u[q * R0]);
+      }
+    }
+    __syncthreads();  // previous pol's last pass has finished reading buf
+    if (active) pass_store<N, R0, 1>(buf, u, tid);
+    __syncthreads();
+    MidPasses<N, R0>::run(buf, prm.tw, u, tid, active);
+    // ---- last radix-16 pass: outputs c = tid + r*N/16 go straight to global
+    if (active) {
+      pass_load<N, 16, N / 16>(buf, prm.tw, u, tid);
+      const int s = 2 * ant + pol;
+#pragma unroll
+      for (int r = 0; r < 16; r++) {
+        const int c = tid + r * (N / 16);
+        if (c < nchan) {
+          const float2 fr = cmul(fsubt[c & prm.fsub_mask], fstept[c >> prm.fsub_shift]);
+          const float2 y = cmul(u[r], fr);
+          const size_t o = (((size_t)(c >> 4) * prm.T + tl) * nstreams + s) * CW + (c & 15);
+          chan[o] = to_out<OutT>(y, prm.out_scale);
+        }
+      }
+    }
+  }
+}
+
+template <int L, typename OutT, bool CPLX>
+static cudaError_t launch_fstage_t(const FParams &prm, int nt, cudaStream_t s) {
+  using Plan = FftPlan<L>;
+  const Job &job = prm.job;
+  const size_t smem = sizeof(float2) * ((size_t)Plan::N + Plan::N / 16 + job.substride + job.stride + job.fsub +
+                                        job.fstride);
+  auto kern = fstage_kernel<L, OutT, CPLX>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((unsigned)nt, (unsigned)job.nant);
+  kern<<<grid, Plan::NT, smem, s>>>(prm);
+  return cudaGetLastError();
+}
+
+template <typename OutT, bool CPLX>
+static cudaError_t launch_fstage_l(const FParams &prm, int nt, cudaStream_t s) {
+  switch (prm.job.log2F) {
+    case 8: return launch_fstage_t<8, OutT, CPLX>(prm, nt, s);
+    case 9: return launch_fstage_t<9, OutT, CPLX>(prm, nt, s);
+    case 10: return launch_fstage_t<10, OutT, CPLX>(prm, nt, s);
+    case 11: return launch_fstage_t<11, OutT, CPLX>(prm, nt, s);
+    case 12: return launch_fstage_t<12, OutT, CPLX>(prm, nt, s);
+    case 13: return launch_fstage_t<13, OutT, CPLX>(prm, nt, s);
+    case 14: return launch_fstage_t<14, OutT, CPLX>(prm, nt, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+int fstage_supported(int F) { return F >= 256 && F <= 16384 && (F & (F - 1)) == 0; }
+
+static int ilog2(int x) {
+  int l = 0;
+  while ((1 << (l + 1)) <= x) l++;
+  return l;
+}
+
+cudaError_t launch_fstage(const Job &job, const float2 *twiddles, int t0, int nt, int T, void *chan, int chan_type,
+                          float out_scale, cudaStream_t s) {
+  if (nt <= 0) return cudaSuccess;
+  FParams prm;
+  prm.job = job;
+  prm.tw = twiddles;
+  prm.t0 = t0;
+  prm.T = T;
+  prm.chan = chan;
+  prm.out_scale = out_scale;
+  prm.sub_shift = ilog2(job.substride);
+  prm.sub_mask = job.substride - 1;
+  prm.fsub_shift = ilog2(job.fsub);
+  prm.fsub_mask = job.fsub - 1;
+  if (chan_type == CHAN_F32) {
+    return job.is_complex ? launch_fstage_l<float2, true>(prm, nt, s) : launch_fstage_l<float2, false>(prm, nt, s);
+  }
+  return job.is_complex ? launch_fstage_l<__half2, true>(prm, nt, s) : launch_fstage_l<__half2, false>(prm, nt, s);
+}
+
+}  // namespace gxc

@@ -1,0 +1,570 @@
+// C ABI of libgxcorr (declared in include/gxc.h): the FxKernel-shaped
+// boundary, argument validation with status codes, device buffers, and the
+// per-sub-integration launch sequence.
+//
+// Reference boundary: fxkernel/src/fxkernel.h:29-64 (FxKernel ctor, setInputData,
+// setDelays, process, accumulate); reference call sequence of a GPU
+// sub-integration: gcorr/src/testgpukernel.cu:462-534.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "gxc_internal.h"
+
+using namespace gxc;
+
+struct gxc_handle {
+  gxc_config cfg;
+  Job job;
+  int device = 0;
+  int F = 0, log2F = 0, nbl = 0, T = 0, nblocks = 0;
+  int chan_type = CHAN_F32;
+  int xeng = GXC_XENGINE_CUDA_CORE;
+  float out_scale = 1.f;   // applied to channelised values before the cast
+  float vis_scale = 1.f;   // 1/out_scale^2, applied at finalisation
+  size_t bytes_per_ant = 0;
+
+  // inputs
+  std::vector<const uint8_t *> user_ptrs;
+  bool input_on_host = false;
+  bool have_input = false, have_delays = false;
+  uint8_t *d_inbuf = nullptr;          // staging for host inputs [nant][bytes_per_ant]
+  const uint8_t **d_inptrs = nullptr;  // device array of per-antenna device pointers
+  double *d_poly = nullptr, *d_fso = nullptr;
+  // pinned upload staging: [nant pointers][nant*3 poly][nant fso]
+  unsigned char *h_stage = nullptr;
+  size_t stage_bytes = 0;
+  cudaEvent_t ev_upload = nullptr;
+  std::vector<double> poly, fso;
+
+  // state
+  Geom *d_geom = nullptr;
+  int32_t *d_counts = nullptr;
+  uint8_t *d_valid = nullptr;
+  float2 *d_tw = nullptr;
+  void *d_chan = nullptr;
+  float2 *d_vsum = nullptr, *d_vcomp = nullptr, *d_vis = nullptr;
+  cudaStream_t last_stream = nullptr;
+  cudaEvent_t ev_done = nullptr;
+  bool processed = false;
+  int launches = 0;
+
+  bool stage_timing = false;
+  std::vector<cudaEvent_t> ev_stage;  // per block: F start, F end (= X start), X end
+  cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+
+  std::string err;
+};
+
+namespace {
+
+gxc_status fail(gxc_handle *h, gxc_status s, const std::string &msg) {
+  if (h) h->err = msg;
+  return s;
+}
+
+gxc_status cuda_fail(gxc_handle *h, cudaError_t e, const char *what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  return fail(h, e == cudaErrorMemoryAllocation ? GXC_ERR_OUT_OF_MEMORY : GXC_ERR_CUDA, m);
+}
+
+#define GXC_CUDA(h, call, what)                          \
+  do {                                                   \
+    cudaError_t e__ = (call);                            \
+    if (e__ != cudaSuccess) return cuda_fail(h, e__, what); \
+  } while (0)
+
+int ilog2i(int x) {
+  int l = 0;
+  while ((1 << (l + 1)) <= x) l++;
+  return l;
+}
+
+bool is_pow2(long long x) { return x > 0 && (x & (x - 1)) == 0; }
+
+int fft_len(const gxc_config *c) { return c->is_complex ? c->nchan : 2 * c->nchan; }
+
+std::string validate(const gxc_config *c, gxc_status *st) {
+  *st = GXC_ERR_INVALID_ARGUMENT;
+  if (!c) return "null config";
+  if (c->nant < 1) return "nant must be >= 1";
+  if (c->nfft < 1) return "nfft must be >= 1";
+  if (c->nchan < 16) return "nchan must be >= 16";
+  if (!(c->nbit == 2 || c->nbit == 8)) return "nbit must be 2 or 8";  // fxkernel.cpp:46-55
+  if (!(c->bw_hz > 0.0) || !isfinite(c->bw_hz)) return "bandwidth must be positive";
+  if (!isfinite(c->lo_hz)) return "LO must be finite";
+  if (c->precision < GXC_PRECISION_FP32 || c->precision > GXC_PRECISION_FP8) return "bad precision";
+  if (c->rotator != GXC_ROTATOR_EXACT && c->rotator != GXC_ROTATOR_FXKERNEL) return "bad rotator";
+  if (c->x_engine < GXC_XENGINE_AUTO || c->x_engine > GXC_XENGINE_TENSOR) return "bad x_engine";
+  if (c->fft_block < 0) return "fft_block must be >= 0";
+  const long long F = fft_len(c);
+  if (!is_pow2(F)) return "FFT length (2*nchan real, nchan complex) must be a power of two";
+  if (c->rotator == GXC_ROTATOR_FXKERNEL) {
+    const int s = (int)sqrt((double)c->nchan);
+    if (s * s != c->nchan) return "the fxkernel rotator needs a square nchan (fxkernel.cpp:58-63)";
+  }
+  if ((long long)c->nfft * F > 2147483647LL) return "nfft*F exceeds the 32-bit sample index of the input format";
+  *st = GXC_ERR_UNSUPPORTED;
+  if (!((c->nbit == 2 && !c->is_complex) || (c->nbit == 8 && c->is_complex)))
+    return "supported input formats: 2-bit real, 8-bit complex";
+  if (!fstage_supported((int)F)) return "FFT length outside 256..16384";
+  if (c->precision == GXC_PRECISION_FP8) return "FP8 channelised data is not implemented";
+  if (c->x_engine == GXC_XENGINE_TENSOR) {
+    if (c->precision != GXC_PRECISION_FP16) return "the tensor-core X-stage takes FP16 channelised data";
+    if (!xstage_tensor_supported(c->nant)) return "tensor-core X-stage: nant outside the supported range";
+  }
+  *st = GXC_OK;
+  return "";
+}
+
+size_t input_bytes(const gxc_config *c) {
+  const size_t F = (size_t)fft_len(c);
+  const size_t comps = c->is_complex ? 2 : 1;
+  return (size_t)(c->nfft + 1) * F * 2u * comps * (size_t)c->nbit / 8u;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gxc_config_init(gxc_config *c) {
+  if (!c) return;
+  memset(c, 0, sizeof(*c));
+  c->nbit = 2;
+  c->precision = GXC_PRECISION_FP32;
+  c->rotator = GXC_ROTATOR_EXACT;
+  c->autos = 1;
+  c->x_engine = GXC_XENGINE_AUTO;
+  c->device = -1;
+}
+
+gxc_status gxc_validate_config(const gxc_config *c) {
+  gxc_status st;
+  validate(c, &st);
+  return st;
+}
+
+size_t gxc_input_bytes_per_antenna(const gxc_config *c) { return c ? input_bytes(c) : 0; }
+
+int gxc_num_baselines(const gxc_config *c) {
+  if (!c || c->nant < 1) return 0;
+  return c->nant * (c->nant - 1) / 2 + (c->autos ? c->nant : 0);
+}
+
+const char *gxc_status_string(gxc_status s) {
+  switch (s) {
+    case GXC_OK: return "ok";
+    case GXC_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GXC_ERR_UNSUPPORTED: return "unsupported";
+    case GXC_ERR_CUDA: return "CUDA error";
+    case GXC_ERR_OUT_OF_MEMORY: return "out of memory";
+    case GXC_ERR_STATE: return "bad call order";
+    case GXC_ERR_TIMEOUT: return "device wait timed out";
+  }
+  return "unknown status";
+}
+
+const char *gxc_last_error(const gxc_handle *h) { return h ? h->err.c_str() : "null handle"; }
+int gxc_last_launch_count(const gxc_handle *h) { return h ? h->launches : 0; }
+int gxc_fft_block(const gxc_handle *h) { return h ? h->T : 0; }
+const float *gxc_device_visibilities(const gxc_handle *h) { return h ? (const float *)h->d_vis : nullptr; }
+
+static void release(gxc_handle *h) {
+  cudaFree(h->d_inbuf);
+  cudaFree((void *)h->d_inptrs);
+  cudaFree(h->d_poly);
+  cudaFree(h->d_fso);
+  cudaFree(h->d_geom);
+  cudaFree(h->d_counts);
+  cudaFree(h->d_valid);
+  cudaFree(h->d_tw);
+  cudaFree(h->d_chan);
+  cudaFree(h->d_vsum);
+  cudaFree(h->d_vcomp);
+  cudaFree(h->d_vis);
+  if (h->h_stage) cudaFreeHost(h->h_stage);
+  if (h->ev_upload) cudaEventDestroy(h->ev_upload);
+  if (h->ev_done) cudaEventDestroy(h->ev_done);
+  for (cudaEvent_t e : h->ev_stage) cudaEventDestroy(e);
+  if (h->ev_begin) cudaEventDestroy(h->ev_begin);
+  if (h->ev_end) cudaEventDestroy(h->ev_end);
+}
+
+gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
+  if (!out) return GXC_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  gxc_status st;
+  std::string msg = validate(cfg, &st);
+  if (st != GXC_OK) {
+    fprintf(stderr, "gxc_create: %s\n", msg.c_str());
+    return st;
+  }
+  gxc_handle *h = new gxc_handle();
+  h->cfg = *cfg;
+  if (cfg->device >= 0) {
+    cudaError_t e = cudaSetDevice(cfg->device);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "gxc_create: cudaSetDevice(%d): %s\n", cfg->device, cudaGetErrorString(e));
+      delete h;
+      return GXC_ERR_CUDA;
+    }
+  }
+  cudaGetDevice(&h->device);
+  const int nant = cfg->nant;
+  h->F = fft_len(cfg);
+  h->log2F = ilog2i(h->F);
+  h->nbl = gxc_num_baselines(cfg);
+  h->bytes_per_ant = input_bytes(cfg);
+  h->chan_type = (cfg->precision == GXC_PRECISION_FP32) ? CHAN_F32 : CHAN_F16;
+  h->xeng = cfg->x_engine;
+  if (h->xeng == GXC_XENGINE_AUTO)
+    h->xeng = (cfg->precision == GXC_PRECISION_FP16 && xstage_tensor_supported(nant)) ? GXC_XENGINE_TENSOR
+                                                                                       : GXC_XENGINE_CUDA_CORE;
+  // FP16 storage keeps |X| near the sample rms: scale by 2^-floor(log2(F)/2),
+  // an exact power of two undone exactly at finalisation.
+  if (h->chan_type == CHAN_F16) {
+    h->out_scale = ldexpf(1.0f, -(h->log2F / 2));
+    h->vis_scale = ldexpf(1.0f, 2 * (h->log2F / 2));
+  }
+  // FFT block: bounded channelised buffer (<= 2 GiB), multiple of 64 FFTs.
+  const size_t esz = h->chan_type == CHAN_F32 ? sizeof(float2) : sizeof(__half2);
+  const size_t per_fft = (size_t)cfg->nchan * 2 * nant * esz;
+  int T = cfg->fft_block;
+  if (T <= 0) {
+    size_t cap = ((size_t)2 << 30) / per_fft;
+    if (cap < 64) cap = 64;
+    T = (int)(cap > (size_t)cfg->nfft ? (size_t)cfg->nfft : cap);
+    if (T > 64) T -= T % 64;
+  }
+  if (T > cfg->nfft) T = cfg->nfft;
+  h->T = T;
+  h->nblocks = (cfg->nfft + T - 1) / T;
+
+  // rotator/frac table split (fxkernel.cpp:57-64; power-of-two split for non-square nchan)
+  int stride = (int)sqrt((double)cfg->nchan);
+  if (stride * stride != cfg->nchan) stride = 1 << (ilog2i(cfg->nchan) / 2);
+  Job &j = h->job;
+  j.nant = nant;
+  j.nchan = cfg->nchan;
+  j.nfft = cfg->nfft;
+  j.F = h->F;
+  j.log2F = h->log2F;
+  j.is_complex = cfg->is_complex;
+  j.rotator = cfg->rotator;
+  j.stride = stride;
+  j.substride = h->F / stride;
+  j.fstride = stride;
+  j.fsub = cfg->nchan / stride;
+  j.fractional_lo = (cfg->lo_hz - (double)(long long)cfg->lo_hz) > 0.00000000001;
+  j.lo_hz = cfg->lo_hz;
+  j.bw_hz = cfg->bw_hz;
+  j.Ts = cfg->is_complex ? 1.0 / cfg->bw_hz : 1.0 / (2.0 * cfg->bw_hz);
+  j.maxoffset = (long long)(cfg->nfft - 1) * h->F;
+
+  cudaError_t e = cudaSuccess;
+  auto A = [&](void **p, size_t n) {
+    if (e == cudaSuccess) e = cudaMalloc(p, n);
+  };
+  A((void **)&h->d_inptrs, sizeof(uint8_t *) * nant);
+  A((void **)&h->d_poly, sizeof(double) * 3 * nant);
+  A((void **)&h->d_fso, sizeof(double) * nant);
+  A((void **)&h->d_geom, sizeof(Geom) * (size_t)nant * cfg->nfft);
+  A((void **)&h->d_counts, sizeof(int32_t) * (h->nbl > 0 ? h->nbl : 1));
+  A((void **)&h->d_valid, (size_t)nant * cfg->nfft);
+  A(&h->d_chan, per_fft * (size_t)T);
+  const size_t nvis = (size_t)(h->nbl > 0 ? h->nbl : 1) * 4 * cfg->nchan;
+  A((void **)&h->d_vsum, sizeof(float2) * nvis);
+  A((void **)&h->d_vcomp, sizeof(float2) * nvis);
+  A((void **)&h->d_vis, sizeof(float2) * nvis);
+  if (e == cudaSuccess) e = make_twiddles(h->F, &h->d_tw);
+  h->stage_bytes = sizeof(uint8_t *) * nant + sizeof(double) * 4 * nant;
+  if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_stage, h->stage_bytes);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_upload, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMemset(h->d_vis, 0, sizeof(float2) * nvis);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gxc_create: %s\n", cudaGetErrorString(e));
+    release(h);
+    delete h;
+    return e == cudaErrorMemoryAllocation ? GXC_ERR_OUT_OF_MEMORY : GXC_ERR_CUDA;
+  }
+  j.inputs = h->d_inptrs;
+  j.poly = h->d_poly;
+  j.fso = h->d_fso;
+  j.geom = h->d_geom;
+  h->poly.assign(3 * (size_t)nant, 0.0);
+  h->fso.assign((size_t)nant, 0.0);
+  *out = h;
+  return GXC_OK;
+}
+
+gxc_status gxc_destroy(gxc_handle *h) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(h->device);
+  if (h->ev_done && h->processed) cudaEventSynchronize(h->ev_done);
+  release(h);
+  delete h;
+  return GXC_OK;
+}
+
+gxc_status gxc_set_input(gxc_handle *h, const uint8_t *const *per_ant, size_t bytes_per_ant) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!per_ant) return fail(h, GXC_ERR_INVALID_ARGUMENT, "null input pointer array");
+  if (bytes_per_ant < h->bytes_per_ant)
+    return fail(h, GXC_ERR_INVALID_ARGUMENT,
+                "input buffers too small: need " + std::to_string(h->bytes_per_ant) + " bytes per antenna");
+  cudaSetDevice(h->device);
+  int n_dev = 0, n_host = 0;
+  for (int a = 0; a < h->cfg.nant; a++) {
+    if (!per_ant[a]) return fail(h, GXC_ERR_INVALID_ARGUMENT, "null input buffer for antenna " + std::to_string(a));
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, per_ant[a]);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      n_host++;
+      continue;
+    }
+    if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) {
+      if (h->cfg.is_complex && ((uintptr_t)per_ant[a] & 1u))
+        return fail(h, GXC_ERR_INVALID_ARGUMENT, "8-bit complex device input must be 2-byte aligned");
+      n_dev++;
+    } else {
+      n_host++;
+    }
+  }
+  if (n_dev && n_host) return fail(h, GXC_ERR_INVALID_ARGUMENT, "inputs must be all host or all device buffers");
+  h->input_on_host = n_host > 0;
+  h->user_ptrs.assign(per_ant, per_ant + h->cfg.nant);
+  if (h->input_on_host && !h->d_inbuf) {
+    cudaError_t e = cudaMalloc((void **)&h->d_inbuf, h->bytes_per_ant * (size_t)h->cfg.nant);
+    if (e != cudaSuccess) return cuda_fail(h, e, "allocating the device input buffer");
+  }
+  h->have_input = true;
+  return GXC_OK;
+}
+
+gxc_status gxc_set_delays(gxc_handle *h, const double *poly, const double *fso) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!poly || !fso) return fail(h, GXC_ERR_INVALID_ARGUMENT, "null delay arrays");
+  memcpy(h->poly.data(), poly, sizeof(double) * 3 * h->cfg.nant);
+  memcpy(h->fso.data(), fso, sizeof(double) * h->cfg.nant);
+  h->have_delays = true;
+  return GXC_OK;
+}
+
+// finalisation: vis = (sum + comp) * scale / count (fxkernel.cpp:358-367)
+__global__ void finalize_kernel(const float2 *__restrict__ vsum, const float2 *__restrict__ vcomp,
+                                const int32_t *__restrict__ counts, int nchan, size_t n, float scale,
+                                float2 *__restrict__ vis) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int bl = (int)(i / ((size_t)4 * nchan));
+  const int cnt = counts[bl];
+  const float2 s = vsum[i], c = vcomp[i];
+  float re = (s.x + c.x) * scale, im = (s.y + c.y) * scale;
+  if (cnt > 0) {
+    re /= (float)cnt;
+    im /= (float)cnt;
+  }
+  vis[i] = make_float2(re, im);
+}
+
+__global__ void add_kernel(float *__restrict__ dst, const float *__restrict__ src, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] += src[i];
+}
+
+gxc_status gxc_process(gxc_handle *h, void *stream) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!h->have_input) return fail(h, GXC_ERR_STATE, "process() before set_input()");
+  if (!h->have_delays) return fail(h, GXC_ERR_STATE, "process() before set_delays()");
+  cudaSetDevice(h->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  const gxc_config &c = h->cfg;
+  const int nant = c.nant;
+  int launches = 0;
+
+  // upload pointers + delay model through pinned staging (wait for the previous upload)
+  GXC_CUDA(h, cudaEventSynchronize(h->ev_upload), "waiting for the previous upload");
+  const uint8_t **sp = (const uint8_t **)h->h_stage;
+  double *spoly = (double *)(h->h_stage + sizeof(uint8_t *) * nant);
+  double *sfso = spoly + 3 * nant;
+  for (int a = 0; a < nant; a++)
+    sp[a] = h->input_on_host ? h->d_inbuf + (size_t)a * h->bytes_per_ant : h->user_ptrs[a];
+  memcpy(spoly, h->poly.data(), sizeof(double) * 3 * nant);
+  memcpy(sfso, h->fso.data(), sizeof(double) * nant);
+  GXC_CUDA(h, cudaMemcpyAsync((void *)h->d_inptrs, sp, sizeof(uint8_t *) * nant, cudaMemcpyHostToDevice, s),
+           "uploading input pointers");
+  GXC_CUDA(h, cudaMemcpyAsync(h->d_poly, spoly, sizeof(double) * 3 * nant, cudaMemcpyHostToDevice, s),
+           "uploading delays");
+  GXC_CUDA(h, cudaMemcpyAsync(h->d_fso, sfso, sizeof(double) * nant, cudaMemcpyHostToDevice, s),
+           "uploading file start offsets");
+  GXC_CUDA(h, cudaEventRecord(h->ev_upload, s), "recording the upload event");
+  if (h->input_on_host) {
+    for (int a = 0; a < nant; a++)
+      GXC_CUDA(h,
+               cudaMemcpyAsync(h->d_inbuf + (size_t)a * h->bytes_per_ant, h->user_ptrs[a], h->bytes_per_ant,
+                               cudaMemcpyHostToDevice, s),
+               "copying input to the device");
+  }
+  if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_begin, s), "timing event");
+
+  GXC_CUDA(h, launch_geometry(h->job, s), "geometry kernel");
+  launches++;
+  if (h->nbl > 0) {
+    GXC_CUDA(h, launch_counts(h->job, c.autos, h->d_counts, h->d_valid, s), "counts kernel");
+    launches++;
+  }
+  const size_t nvis = (size_t)h->nbl * 4 * c.nchan;
+  GXC_CUDA(h, cudaMemsetAsync(h->d_vsum, 0, sizeof(float2) * nvis, s), "clearing accumulators");
+  GXC_CUDA(h, cudaMemsetAsync(h->d_vcomp, 0, sizeof(float2) * nvis, s), "clearing accumulators");
+
+  if (h->stage_timing && h->ev_stage.size() != (size_t)3 * h->nblocks) {
+    for (cudaEvent_t e : h->ev_stage) cudaEventDestroy(e);
+    h->ev_stage.assign((size_t)3 * h->nblocks, nullptr);
+    for (auto &e : h->ev_stage) GXC_CUDA(h, cudaEventCreate(&e), "timing event");
+  }
+  for (int b = 0; b < h->nblocks; b++) {
+    const int t0 = b * h->T;
+    const int nt = (c.nfft - t0) < h->T ? (c.nfft - t0) : h->T;
+    if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b], s), "timing event");
+    GXC_CUDA(h, launch_fstage(h->job, h->d_tw, t0, nt, h->T, h->d_chan, h->chan_type, h->out_scale, s),
+             "F-stage kernel");
+    launches++;
+    if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b + 1], s), "timing event");
+    if (h->nbl > 0) {
+      if (h->xeng == GXC_XENGINE_TENSOR) {
+        GXC_CUDA(h, launch_xstage_tensor(h->d_chan, nant, c.nchan, h->T, nt, c.autos, h->d_vsum, h->d_vcomp, s),
+                 "tensor-core X-stage kernel");
+      } else {
+        GXC_CUDA(h,
+                 launch_xstage_cuda_core(h->d_chan, h->chan_type, nant, c.nchan, h->T, nt, c.autos, h->d_vsum,
+                                         h->d_vcomp, s),
+                 "X-stage kernel");
+      }
+      launches++;
+    }
+    if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b + 2], s), "timing event");
+  }
+  if (nvis > 0) {
+    const int th = 256;
+    finalize_kernel<<<(unsigned)((nvis + th - 1) / th), th, 0, s>>>(h->d_vsum, h->d_vcomp, h->d_counts, c.nchan,
+                                                                     nvis, h->vis_scale, h->d_vis);
+    GXC_CUDA(h, cudaGetLastError(), "finalize kernel");
+    launches++;
+  }
+  if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_end, s), "timing event");
+  GXC_CUDA(h, cudaEventRecord(h->ev_done, s), "recording the completion event");
+  h->last_stream = s;
+  h->processed = true;
+  h->launches = launches;
+  return GXC_OK;
+}
+
+gxc_status gxc_sync(gxc_handle *h) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!h->processed) return GXC_OK;
+  cudaSetDevice(h->device);
+  GXC_CUDA(h, cudaEventSynchronize(h->ev_done), "synchronising");
+  GXC_CUDA(h, cudaGetLastError(), "device error");
+  return GXC_OK;
+}
+
+static bool is_device_ptr(const void *p) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+gxc_status gxc_get_visibilities(gxc_handle *h, float *out) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!out) return fail(h, GXC_ERR_INVALID_ARGUMENT, "null output");
+  if (!h->processed) return fail(h, GXC_ERR_STATE, "no processed sub-integration");
+  gxc_status st = gxc_sync(h);
+  if (st != GXC_OK) return st;
+  const size_t n = (size_t)h->nbl * 4 * h->cfg.nchan * 2;
+  GXC_CUDA(h, cudaMemcpy(out, h->d_vis, n * sizeof(float), cudaMemcpyDefault), "copying visibilities");
+  return GXC_OK;
+}
+
+gxc_status gxc_accumulate(gxc_handle *h, float *odata) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!odata) return fail(h, GXC_ERR_INVALID_ARGUMENT, "null output");
+  if (!h->processed) return fail(h, GXC_ERR_STATE, "no processed sub-integration");
+  gxc_status st = gxc_sync(h);
+  if (st != GXC_OK) return st;
+  const size_t n = (size_t)h->nbl * 4 * h->cfg.nchan * 2;
+  if (is_device_ptr(odata)) {
+    const int th = 256;
+    add_kernel<<<(unsigned)((n + th - 1) / th), th, 0, h->last_stream>>>(odata, (const float *)h->d_vis, n);
+    GXC_CUDA(h, cudaGetLastError(), "accumulate kernel");
+    GXC_CUDA(h, cudaStreamSynchronize(h->last_stream), "accumulate");
+  } else {
+    std::vector<float> tmp(n);
+    GXC_CUDA(h, cudaMemcpy(tmp.data(), h->d_vis, n * sizeof(float), cudaMemcpyDeviceToHost), "copying visibilities");
+    for (size_t i = 0; i < n; i++) odata[i] += tmp[i];
+  }
+  return GXC_OK;
+}
+
+gxc_status gxc_get_baseline_counts(gxc_handle *h, int32_t *counts) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!counts) return fail(h, GXC_ERR_INVALID_ARGUMENT, "null output");
+  if (!h->processed) return fail(h, GXC_ERR_STATE, "no processed sub-integration");
+  gxc_status st = gxc_sync(h);
+  if (st != GXC_OK) return st;
+  if (h->nbl > 0)
+    GXC_CUDA(h, cudaMemcpy(counts, h->d_counts, sizeof(int32_t) * h->nbl, cudaMemcpyDeviceToHost), "copying counts");
+  return GXC_OK;
+}
+
+gxc_status gxc_get_valid_flags(gxc_handle *h, uint8_t *flags) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!flags) return fail(h, GXC_ERR_INVALID_ARGUMENT, "null output");
+  if (!h->processed) return fail(h, GXC_ERR_STATE, "no processed sub-integration");
+  if (h->nbl == 0) return fail(h, GXC_ERR_STATE, "no baselines: flags are not exported");
+  gxc_status st = gxc_sync(h);
+  if (st != GXC_OK) return st;
+  GXC_CUDA(h, cudaMemcpy(flags, h->d_valid, (size_t)h->cfg.nant * h->cfg.nfft, cudaMemcpyDeviceToHost),
+           "copying flags");
+  return GXC_OK;
+}
+
+gxc_status gxc_enable_stage_timing(gxc_handle *h, int enable) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(h->device);
+  h->stage_timing = enable != 0;
+  if (h->stage_timing && !h->ev_begin) {
+    GXC_CUDA(h, cudaEventCreate(&h->ev_begin), "timing event");
+    GXC_CUDA(h, cudaEventCreate(&h->ev_end), "timing event");
+  }
+  return GXC_OK;
+}
+
+gxc_status gxc_stage_times(gxc_handle *h, float *f_ms, float *x_ms, float *total_ms) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!h->stage_timing || !h->processed) return fail(h, GXC_ERR_STATE, "stage timing not enabled/recorded");
+  gxc_status st = gxc_sync(h);
+  if (st != GXC_OK) return st;
+  float fs = 0.f, xs = 0.f, tot = 0.f;
+  for (int b = 0; b < h->nblocks; b++) {
+    float a = 0.f, x = 0.f;
+    GXC_CUDA(h, cudaEventElapsedTime(&a, h->ev_stage[3 * b], h->ev_stage[3 * b + 1]), "timing");
+    GXC_CUDA(h, cudaEventElapsedTime(&x, h->ev_stage[3 * b + 1], h->ev_stage[3 * b + 2]), "timing");
+    fs += a;
+    xs += x;
+  }
+  GXC_CUDA(h, cudaEventElapsedTime(&tot, h->ev_begin, h->ev_end), "timing");
+  if (f_ms) *f_ms = fs;
+  if (x_ms) *x_ms = xs;
+  if (total_ms) *total_ms = tot;
+  return GXC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,80 @@
+// Internal declarations shared by the libgxcorr translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "gxc.h"
+
+namespace gxc {
+
+// Channels per channel tile of the channelised layout [ctile][t][stream][CW].
+constexpr int CW = 16;
+
+// Per-(antenna, FFT) geometry record, produced by the geometry kernel from the
+// delay polynomial (fxkernel/src/fxkernel.cpp:288-309, :425-440).
+struct Geom {
+  double a;      // delay gradient across the FFT (s per FFT interval)
+  double b;      // delay at the start of the FFT (s)
+  double frac;   // residual fractional delay (s)
+  int offset;    // first sample of the FFT window in the antenna stream
+  int valid;     // 0 = flagged (window outside the buffer)
+};
+static_assert(sizeof(Geom) == 32, "Geom layout");
+
+// Launch-time description of one sub-integration for the device kernels.
+struct Job {
+  const uint8_t *const *inputs;  // device array of nant device pointers
+  const double *poly;            // [nant][3]
+  const double *fso;             // [nant]
+  Geom *geom;                    // [nant][nfft]
+  int nant, nchan, nfft, F, log2F;
+  int is_complex;                // 0: 2-bit real, 1: 8-bit complex
+  int rotator;                   // GXC_ROTATOR_*
+  int stride, substride;         // fringe rotator table split: F = stride * substride
+  int fsub, fstride;             // frac-delay table split: nchan = fstride * fsub
+  int fractional_lo;             // fxkernel.cpp:67-71
+  double lo_hz, bw_hz, Ts;
+  long long maxoffset;           // (nfft-1)*F
+};
+
+// Channelised-data element types.
+enum ChanType { CHAN_F32 = 0, CHAN_F16 = 1 };
+
+// fstage.cu
+cudaError_t launch_geometry(const Job &job, cudaStream_t s);
+cudaError_t launch_counts(const Job &job, int autos, int32_t *counts, uint8_t *valid_flags, cudaStream_t s);
+cudaError_t make_twiddles(int F, float2 **out);
+cudaError_t launch_fstage(const Job &job, const float2 *twiddles, int t0, int nt, int T, void *chan, int chan_type,
+                          float out_scale, cudaStream_t s);
+int fstage_supported(int F);
+
+// xstage_fp32.cu: accumulates visibilities of FFTs [0, nt) of the block into
+// the compensated (sum, comp) accumulators in the output layout.
+cudaError_t launch_xstage_cuda_core(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,
+                                    float2 *vsum, float2 *vcomp, cudaStream_t s);
+
+// xstage_tc.cu: tcgen05 tensor-core X-stage over FP16 channelised data.
+cudaError_t launch_xstage_tensor(const void *chan, int nant, int nchan, int T, int nt, int autos, float2 *vsum,
+                                 float2 *vcomp, cudaStream_t s);
+int xstage_tensor_supported(int nant);
+
+// Output baseline index of antennas j <= k (crosses in fxkernel order, then autos).
+__host__ __device__ inline int baseline_index(int j, int k, int nant) {
+  if (j == k) return nant * (nant - 1) / 2 + j;
+  return j * nant - j * (j + 1) / 2 + (k - j - 1);
+}
+
+// Compensated accumulation acc += x (TwoSum): sum holds the running total,
+// comp the accumulated rounding error; the result is sum + comp.
+__device__ inline void two_sum_add(float &sum, float &comp, float x) {
+  float t = sum + x;
+  float bp = t - sum;
+  float e = (sum - (t - bp)) + (x - bp);
+  sum = t;
+  comp += e;
+}
+
+}  // namespace gxc

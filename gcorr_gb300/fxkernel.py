@@ -1,0 +1,171 @@
+"""Python host mirror of the reference FxKernel API over the libgxcorr C ABI.
+
+Same names, argument meaning and error behaviour as fxkernel/src/fxkernel.h:29-64
+(``FxKernel(nant, nchan, nfft, nbit, lo, bw, is_complex)``, ``setInputData``,
+``setDelays``, ``process``, ``accumulate``, ``saveVisibilities``), except that
+invalid configurations raise ``ValueError`` instead of calling ``exit(1)``
+(fxkernel/src/fxkernel.cpp:46-63).  All compute runs in libgxcorr.so on the GPU;
+there is no CPU fallback: if the library or a GPU is missing, construction fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+PRECISION = {"fp32": L.GXC_PRECISION_FP32, "fp16": L.GXC_PRECISION_FP16, "fp8": L.GXC_PRECISION_FP8}
+ROTATOR = {"exact": L.GXC_ROTATOR_EXACT, "fxkernel": L.GXC_ROTATOR_FXKERNEL}
+XENGINE = {"auto": L.GXC_XENGINE_AUTO, "cuda_core": L.GXC_XENGINE_CUDA_CORE, "tensor": L.GXC_XENGINE_TENSOR}
+
+
+def make_config(nant, nchan, nfft, nbit=2, lo=8.4e9, bw=64e6, is_complex=False, precision="fp32",
+                rotator="exact", autos=True, x_engine="auto", fft_block=0, device=-1) -> L.GxcConfig:
+    cfg = L.GxcConfig()
+    L.lib().gxc_config_init(C.byref(cfg))
+    cfg.nant, cfg.nchan, cfg.nfft, cfg.nbit = int(nant), int(nchan), int(nfft), int(nbit)
+    cfg.is_complex = int(bool(is_complex))
+    cfg.lo_hz, cfg.bw_hz = float(lo), float(bw)
+    cfg.precision = PRECISION[precision] if isinstance(precision, str) else int(precision)
+    cfg.rotator = ROTATOR[rotator] if isinstance(rotator, str) else int(rotator)
+    cfg.autos = int(bool(autos))
+    cfg.x_engine = XENGINE[x_engine] if isinstance(x_engine, str) else int(x_engine)
+    cfg.fft_block = int(fft_block)
+    cfg.device = int(device)
+    return cfg
+
+
+def _ptr(x) -> int:
+    """Address of a numpy array, torch tensor, or an integer address."""
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    if isinstance(x, np.ndarray):
+        return int(x.ctypes.data)
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+class FxKernel:
+    """GPU FX correlator for one sub-integration at a time (FxKernel drop-in)."""
+
+    def __init__(self, nant: int, nchan: int, nfft: int, nbit: int, lo: float, bw: float, is_complex: bool = False,
+                 *, precision: str = "fp32", rotator: str = "exact", autos: bool = True, x_engine: str = "auto",
+                 fft_block: int = 0, device: int = -1):
+        self.cfg = make_config(nant, nchan, nfft, nbit, lo, bw, is_complex, precision, rotator, autos, x_engine,
+                               fft_block, device)
+        st = L.lib().gxc_validate_config(C.byref(self.cfg))
+        if st != L.GXC_OK:
+            raise ValueError(f"invalid FxKernel configuration ({L.status_name(st)})")
+        h = C.c_void_p()
+        st = L.lib().gxc_create(C.byref(self.cfg), C.byref(h))
+        L.check(st, None, "gxc_create")
+        self._h = h
+        self.nant, self.nchan, self.nfft = int(nant), int(nchan), int(nfft)
+        self.nbaselines = L.lib().gxc_num_baselines(C.byref(self.cfg))
+        self.bw = float(bw)
+        self._keep = None
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            L.lib().gxc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- reference API
+    @property
+    def bytes_per_antenna(self) -> int:
+        return int(L.lib().gxc_input_bytes_per_antenna(C.byref(self.cfg)))
+
+    def setInputData(self, idata: Sequence):
+        """idata[a]: uint8 buffer (numpy array, torch tensor on host or GPU, or address)."""
+        if len(idata) != self.nant:
+            raise ValueError(f"need {self.nant} input buffers")
+        ptrs = (C.c_void_p * self.nant)(*[_ptr(x) for x in idata])
+        sizes = []
+        for x in idata:
+            if hasattr(x, "numel"):
+                sizes.append(int(x.numel()) * int(x.element_size()))
+            elif isinstance(x, np.ndarray):
+                sizes.append(int(x.nbytes))
+        nbytes = min(sizes) if sizes else self.bytes_per_antenna
+        self._keep = list(idata)  # the engine borrows the buffers
+        L.check(L.lib().gxc_set_input(self._h, ptrs, C.c_size_t(nbytes)), self._h, "setInputData")
+
+    def setDelays(self, delays, filestartoffsets):
+        poly = np.ascontiguousarray(np.asarray(delays, dtype=np.float64).reshape(self.nant, 3))
+        fso = np.ascontiguousarray(np.asarray(filestartoffsets, dtype=np.float64).reshape(self.nant))
+        L.check(L.lib().gxc_set_delays(self._h, poly.ctypes.data, fso.ctypes.data), self._h, "setDelays")
+
+    def process(self, stream: Optional[int] = None, sync: bool = True):
+        """One sub-integration; ``stream`` is a cudaStream_t address (torch: stream.cuda_stream)."""
+        L.check(L.lib().gxc_process(self._h, C.c_void_p(stream or 0)), self._h, "process")
+        if sync:
+            self.sync()
+
+    def sync(self):
+        L.check(L.lib().gxc_sync(self._h), self._h, "sync")
+
+    def accumulate(self, odata):
+        """odata[nbl][4][nchan] complex64 (numpy or torch, host or GPU) += visibilities."""
+        if isinstance(odata, np.ndarray):
+            if odata.dtype != np.complex64 or not odata.flags.c_contiguous:
+                raise TypeError("odata must be a C-contiguous complex64 array")
+            if odata.size < self.nbaselines * 4 * self.nchan:
+                raise ValueError("odata too small")
+        L.check(L.lib().gxc_accumulate(self._h, C.c_void_p(_ptr(odata))), self._h, "accumulate")
+
+    def visibilities(self) -> np.ndarray:
+        out = np.zeros((self.nbaselines, 4, self.nchan), dtype=np.complex64)
+        L.check(L.lib().gxc_get_visibilities(self._h, C.c_void_p(out.ctypes.data)), self._h, "get_visibilities")
+        return out
+
+    def device_visibilities_ptr(self) -> int:
+        return int(L.lib().gxc_device_visibilities(self._h) or 0)
+
+    def baseline_counts(self) -> np.ndarray:
+        out = np.zeros(self.nbaselines, dtype=np.int32)
+        L.check(L.lib().gxc_get_baseline_counts(self._h, C.c_void_p(out.ctypes.data)), self._h, "counts")
+        return out
+
+    def valid_flags(self) -> np.ndarray:
+        out = np.zeros((self.nant, self.nfft), dtype=np.uint8)
+        L.check(L.lib().gxc_get_valid_flags(self._h, C.c_void_p(out.ctypes.data)), self._h, "valid_flags")
+        return out
+
+    def saveVisibilities(self, outfile: str):
+        """Text dump in the reference format (fxkernel/src/fxkernel.cpp:370-412)."""
+        from .visio import save_visibilities
+        save_visibilities(outfile, self.visibilities(), self.bw)
+
+    # -- accounting
+    @property
+    def launches(self) -> int:
+        return int(L.lib().gxc_last_launch_count(self._h))
+
+    @property
+    def fft_block(self) -> int:
+        return int(L.lib().gxc_fft_block(self._h))
+
+    def enable_stage_timing(self, on: bool = True):
+        L.check(L.lib().gxc_enable_stage_timing(self._h, int(on)), self._h, "stage timing")
+
+    def stage_times(self):
+        f, x, t = C.c_float(), C.c_float(), C.c_float()
+        L.check(L.lib().gxc_stage_times(self._h, C.byref(f), C.byref(x), C.byref(t)), self._h, "stage times")
+        return float(f.value), float(x.value), float(t.value)

@@ -1,0 +1,132 @@
+/*
+ * gxc.h — C ABI of the GB300 FX correlator engine (libgxcorr.so).
+ *
+ * This is the drop-in boundary for the reference's FxKernel API
+ * (fxkernel/src/fxkernel.h:29-64): configure antennas, channels and the delay
+ * model, process one sub-integration of packed dual-pol voltages, accumulate
+ * visibilities.  Plain C types only (a CUDA stream is passed as void*), status
+ * codes instead of exit(), caller-owned buffers, all device work on the
+ * caller's stream.  A handle is not thread-safe: use one per host thread, as
+ * the reference uses one FxKernel per thread (fxkernel/src/bench_fxkernel.cpp:93-139).
+ *
+ * Input format (per antenna, one buffer of (nfft+1) FFT windows):
+ *   2-bit real:    4 samples per byte, A_t | B_t<<2 | A_t+1<<4 | B_t+1<<6,
+ *                  levels {-3.3359,-1,+1,+3.3359} (fxkernel/src/fxkernel.cpp:15-28);
+ *                  nchan*(nfft+1) bytes, as fxkernel/src/common.cpp:82.
+ *   8-bit complex: int8 A.re, A.im, B.re, B.im per time sample;
+ *                  4*nchan*(nfft+1) bytes.
+ * Delay model: per antenna poly[3] = coefficients of t^2, t, 1 (seconds, t in
+ *   FFT intervals) and a file-start offset fso (seconds) (fxkernel/src/common.h:38-39).
+ * Output layout GXC_LAYOUT_FXKERNEL: complex float (re,im interleaved)
+ *   [nbl][4][nchan]; cross baselines in fxkernel order (0,1),(0,2)..(nant-2,nant-1)
+ *   (fxkernel/src/fxkernel.cpp:328-355), products AA,AB,BA,BB = X_j,l * conj(X_k,m);
+ *   when autos are on, nant auto baselines (0,0),(1,1).. follow.
+ *   Each baseline is divided by its count of FFTs where both antennas were
+ *   valid (fxkernel/src/fxkernel.cpp:358-367).
+ */
+#ifndef GXC_H
+#define GXC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gxc_status {
+  GXC_OK = 0,
+  GXC_ERR_INVALID_ARGUMENT = 1, /* bad configuration or argument (reference: exit(1), fxkernel.cpp:46-63) */
+  GXC_ERR_UNSUPPORTED = 2,      /* valid request this build does not implement */
+  GXC_ERR_CUDA = 3,             /* a CUDA runtime call failed; see gxc_last_error */
+  GXC_ERR_OUT_OF_MEMORY = 4,
+  GXC_ERR_STATE = 5,            /* call order: process() before set_input()/set_delays() */
+  GXC_ERR_TIMEOUT = 6           /* a bounded device-side wait gave up */
+} gxc_status;
+
+enum { GXC_PRECISION_FP32 = 0, GXC_PRECISION_FP16 = 1, GXC_PRECISION_FP8 = 2 };
+/* EXACT: linear fringe phase per sample; FXKERNEL: the reference's sub/step
+ * rotator table including its real-data half-rate step (fxkernel.cpp:112,553-558). */
+enum { GXC_ROTATOR_EXACT = 0, GXC_ROTATOR_FXKERNEL = 1 };
+/* X-stage engine: AUTO picks tensor cores for FP16/FP8 and CUDA cores for FP32. */
+enum { GXC_XENGINE_AUTO = 0, GXC_XENGINE_CUDA_CORE = 1, GXC_XENGINE_TENSOR = 2 };
+enum { GXC_LAYOUT_FXKERNEL = 0 };
+
+typedef struct gxc_config {
+  int nant;        /* antennas (>= 1) */
+  int nchan;       /* output channels; FFT length is 2*nchan (real) or nchan (complex), a power of two */
+  int nfft;        /* FFTs per sub-integration */
+  int nbit;        /* 2 (real) or 8 (complex) */
+  int is_complex;  /* 0 real-sampled, 1 complex-sampled */
+  double lo_hz;    /* local oscillator frequency (Hz) */
+  double bw_hz;    /* bandwidth (Hz) */
+  int precision;   /* GXC_PRECISION_*: element type of the channelised data fed to the X-stage */
+  int rotator;     /* GXC_ROTATOR_* */
+  int autos;       /* 1: append autocorrelations */
+  int x_engine;    /* GXC_XENGINE_* */
+  int fft_block;   /* FFTs per F/X pass; 0 = automatic */
+  int device;      /* CUDA device ordinal; -1 = current device */
+} gxc_config;
+
+typedef struct gxc_handle gxc_handle;
+
+/* Defaults: 2-bit real, FP32, exact rotator, autos on, automatic engine and block. */
+void gxc_config_init(gxc_config *cfg);
+/* Checks a configuration without touching the GPU. */
+gxc_status gxc_validate_config(const gxc_config *cfg);
+/* Bytes of packed input per antenna for one sub-integration (see header comment). */
+size_t gxc_input_bytes_per_antenna(const gxc_config *cfg);
+/* Output baselines: nant*(nant-1)/2 crosses (+ nant autos when enabled). */
+int gxc_num_baselines(const gxc_config *cfg);
+const char *gxc_status_string(gxc_status s);
+
+/* FxKernel::FxKernel (fxkernel/src/fxkernel.cpp:30-180): allocates device state. */
+gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out);
+/* FxKernel::~FxKernel. */
+gxc_status gxc_destroy(gxc_handle *h);
+
+/* FxKernel::setInputData (fxkernel/src/fxkernel.cpp:242-245): per_ant[a] points at
+ * bytes_per_ant bytes for antenna a, host (pageable or pinned) or device memory.
+ * Device buffers are borrowed and must outlive process(); host buffers are
+ * copied to the device inside every process() call (host->device on the stream). */
+gxc_status gxc_set_input(gxc_handle *h, const uint8_t *const *per_ant, size_t bytes_per_ant);
+/* FxKernel::setDelays (fxkernel/src/fxkernel.cpp:247-251): poly [nant][3], fso [nant]
+ * (host memory).  Values are copied at this call. */
+gxc_status gxc_set_delays(gxc_handle *h, const double *poly, const double *fso);
+/* FxKernel::process (fxkernel/src/fxkernel.cpp:253-368): one sub-integration,
+ * enqueued asynchronously on `stream` (a cudaStream_t; NULL = default stream).
+ * Overwrites the handle's visibilities. */
+gxc_status gxc_process(gxc_handle *h, void *stream);
+/* Waits for the last process() on its stream. */
+gxc_status gxc_sync(gxc_handle *h);
+/* FxKernel::accumulate (fxkernel/src/fxkernel.cpp:414-423): odata += visibilities,
+ * odata complex float [nbl][4][nchan], host or device memory.  Synchronises. */
+gxc_status gxc_accumulate(gxc_handle *h, float *odata);
+/* Copies (not adds) the visibilities into out (host or device), synchronising. */
+gxc_status gxc_get_visibilities(gxc_handle *h, float *out);
+/* Device pointer of the handle's visibility buffer (valid until the next
+ * process() or destroy); complex float [nbl][4][nchan]. */
+const float *gxc_device_visibilities(const gxc_handle *h);
+/* Per-baseline count of FFTs where both antennas were valid (int32 [nbl], host). */
+gxc_status gxc_get_baseline_counts(gxc_handle *h, int32_t *counts);
+/* Per-(antenna, FFT) validity flags (uint8 [nant][nfft], host), the reference's antValid. */
+gxc_status gxc_get_valid_flags(gxc_handle *h, uint8_t *flags);
+/* Text message of the last failing call on this handle ("" if none). */
+const char *gxc_last_error(const gxc_handle *h);
+
+/* Number of kernel launches the last process() enqueued (for accounting). */
+int gxc_last_launch_count(const gxc_handle *h);
+/* Effective FFT block (FFTs per F/X pass) chosen for this handle. */
+int gxc_fft_block(const gxc_handle *h);
+
+/* Stage timing: when enabled, process() records CUDA events around the F-stage
+ * and X-stage launches; gxc_stage_times returns the summed milliseconds of the
+ * last process() (f_ms, x_ms, other_ms).  Synchronises. */
+gxc_status gxc_enable_stage_timing(gxc_handle *h, int enable);
+gxc_status gxc_stage_times(gxc_handle *h, float *f_ms, float *x_ms, float *total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GXC_H */
