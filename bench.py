@@ -162,7 +162,7 @@ def cpu_port_run(w, nfft_sample: int, nthreads: int, seed_inputs=None):
 def cpu_sample(w, budget_s: float = 12.0):
     """Picks a bounded FFT sample taking about budget_s of CPU work on all threads."""
     nthreads = os.cpu_count() or 1
-    n = max(nthreads, 1)
+    n = 8 * nthreads
     rate, dt, _ = cpu_port_run(w, n, nthreads)
     per_fft = dt / n
     n2 = int(max(n, min(w.nfft, budget_s / max(per_fft, 1e-6))))
@@ -222,6 +222,7 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16"])
     ap.add_argument("--x-engine", default="auto", choices=["auto", "cuda_core", "tensor"])
     ap.add_argument("--fft-block", type=int, default=0)
+    ap.add_argument("--nfft", type=int, default=0, help="override the FFT count (small profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--ref-step-s", type=float, default=6.0)
@@ -242,6 +243,8 @@ def main():
     dist = init_dist(world, "nccl")
     dev = torch.device("cuda", local)
     w = synth.Workload(**{**workload(args.config).__dict__, "seed": 1234 + 7919 * rank})
+    if args.nfft > 0:
+        w = synth.Workload(**{**w.__dict__, "nfft": args.nfft})
     tg = time.perf_counter()
     d = synth.generate(w, device=dev)
     torch.cuda.synchronize()

@@ -470,6 +470,11 @@ gxc_status gxc_sync(gxc_handle *h) {
   cudaSetDevice(h->device);
   GXC_CUDA(h, cudaEventSynchronize(h->ev_done), "synchronising");
   GXC_CUDA(h, cudaGetLastError(), "device error");
+  if (h->xeng == GXC_XENGINE_TENSOR) {
+    int flag = 0;
+    GXC_CUDA(h, xstage_tensor_take_error(&flag), "reading the X-stage status");
+    if (flag) return fail(h, GXC_ERR_TIMEOUT, "tensor-core X-stage: a bounded device wait expired");
+  }
   return GXC_OK;
 }
 

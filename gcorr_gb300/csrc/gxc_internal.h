@@ -60,6 +60,7 @@ cudaError_t launch_xstage_cuda_core(const void *chan, int chan_type, int nant, i
 cudaError_t launch_xstage_tensor(const void *chan, int nant, int nchan, int T, int nt, int autos, float2 *vsum,
                                  float2 *vcomp, cudaStream_t s);
 int xstage_tensor_supported(int nant);
+cudaError_t xstage_tensor_take_error(int *flag);
 
 // Output baseline index of antennas j <= k (crosses in fxkernel order, then autos).
 __host__ __device__ inline int baseline_index(int j, int k, int nant) {

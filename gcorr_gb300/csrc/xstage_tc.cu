@@ -1,12 +1,391 @@
-// tcgen05 tensor-core X-stage (FP16 channelised data, FP32 accumulation in TMEM).
+// tcgen05 tensor-core X-stage: per-channel visibility matrix V_c = X_c X_c^H
+// over all streams (antenna x pol) and the FFTs of one block, FP16 inputs,
+// FP32 accumulation in tensor memory (TMEM).
+//
+// Restates the baseline CMAC of FxKernel::process (fxkernel/src/fxkernel.cpp:328-355)
+// as a real Gram matrix: with P_c = [Re X_c ; Im X_c] interleaved by row
+// (row 2s = Re X_s, row 2s+1 = Im X_s, s = 2*ant + pol) and K = time,
+//   G = P_c P_c^T,  Re V[s1][s2] = G[2s1][2s2] + G[2s1+1][2s2+1],
+//                   Im V[s1][s2] = G[2s1+1][2s2] - G[2s1][2s2+1].
+// One M=N=128, K=16 MMA (kind::f16, A and B the same K-major SW128 smem tile)
+// covers g = 128/R channels stacked block-diagonally (R = rows per channel,
+// padded to a power of two >= 16); four such groups fill the 512 TMEM columns,
+// so a CTA owns CS = 4g channels for the whole FFT block.
+//
+// Roles (288 threads): warps 0-7 load the channelised block from global memory
+// (16-byte loads, [ctile][t][stream][16] half2 layout), corner-turn it in
+// registers into K-contiguous rows and store it swizzled into a 3-stage smem
+// ring; warp 8 allocates TMEM and one lane issues the MMAs and commits to the
+// stage-release barriers; warps 0-3 then read TMEM (tcgen05.ld) and fold the
+// Gram entries into the compensated visibility accumulators.
+// Every mbarrier wait is bounded (iteration cap and %globaltimer); on expiry
+// the kernel raises an error flag, lets issued MMAs drain, frees TMEM and exits.
+#include <stdint.h>
+
 #include "gxc_internal.h"
 
 namespace gxc {
 
-int xstage_tensor_supported(int nant) { (void)nant; return 0; }
+namespace tc {
 
-cudaError_t launch_xstage_tensor(const void *, int, int, int, int, int, float2 *, float2 *, cudaStream_t) {
-  return cudaErrorNotSupported;
+constexpr int KC = 64;            // FFTs (K) per smem stage: one 128-byte swizzle row of FP16
+constexpr int NG = 4;             // MMA groups (128 TMEM columns each)
+constexpr int STAGES = 3;
+constexpr int GROUP_BYTES = 128 * 128;           // 128 rows x 128 bytes
+constexpr int STAGE_BYTES = NG * GROUP_BYTES;    // 64 KiB
+constexpr int NPROD_WARPS = 8;
+constexpr int NPROD = NPROD_WARPS * 32;
+constexpr int NTHREADS = NPROD + 32;
+constexpr int TMEM_COLS = 512;
+constexpr unsigned long long WAIT_NS = 4000000000ull;  // 4 s
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false (and the error flag set) if the phase does not complete in time.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (uint32_t i = 0; i < (1u << 26); i++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255u) == 255u) {
+      if (globaltimer() - t0 > WAIT_NS) break;
+      if (*(volatile int *)err) return false;  // another role already gave up
+    }
+  }
+  atomicExch(err, 1);
+  return false;
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, kind::f16 (FP16 in, FP32 accumulate).
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Arrives on the mbarrier once every previously issued tcgen05.mma of this thread completed.
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row core groups
+// 1024 bytes apart (SBO), LBO unused for this layout, descriptor version 1.
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;            // LBO (16 B, ignored for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;  // SBO
+  d |= (uint64_t)1 << 46;            // version
+  d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = F16, both K-major, M = N = 128.
+constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+  uint32_t r;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+  return r;
+}
+
+struct Params {
+  const __half2 *chan;  // [ctile][T][n][16]
+  int nant, nstream, nchan, T, nt, autos;
+  int R, g, CS;         // rows per channel block, channels per MMA group, channels per CTA
+  float2 *vsum, *vcomp;
+  int *err;
+};
+
+__global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_done;
+  __shared__ uint32_t tmem_base_sh;
+  // 128-byte swizzle atoms need 1024-byte alignment of the shared-window address
+  unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t sbase = smem_u32(smem);
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int cb = blockIdx.x * p.CS;  // first channel of this CTA
+  const int n = p.nstream;
+  const int nchunks = (p.nt + KC - 1) / KC;
+
+  // zero the ring once: rows beyond 2n inside each channel block stay zero
+  for (int i = tid; i < STAGES * STAGE_BYTES / 16; i += NTHREADS)
+    reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(smem_u32(&bar_full[s]), NPROD);
+      mbar_init(smem_u32(&bar_empty[s]), 1);
+    }
+    mbar_init(smem_u32(&bar_done), 1);
+    fence_mbar_init();
+  }
+  if (warp == NPROD_WARPS) {
+    tmem_alloc(smem_u32(&tmem_base_sh), TMEM_COLS);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+
+  if (warp < NPROD_WARPS) {
+    // ------------------------------------------------------------ producers
+    const int nq = p.CS / 4;                  // channel quads of this CTA
+    const int ntask = 8 * n * nq;             // (octet, stream, quad) per chunk
+    for (int ch = 0; ch < nchunks; ch++) {
+      const int st = ch % STAGES;
+      if (ch >= STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err)) break;
+      unsigned char *stage = smem + (size_t)st * STAGE_BYTES;
+      const int tb = ch * KC;
+      for (int task = tid; task < ntask; task += NPROD) {
+        const int q = task % nq;
+        const int rest = task / nq;
+        const int s = rest % n;
+        const int o = rest / n;
+        const int c = cb + 4 * q;
+        const int ctile = c >> 4, coff = c & 15;
+        const __half2 *src = p.chan + ((size_t)ctile * p.T * n + s) * CW + coff;
+        uint4 v[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const int t = tb + 8 * o + i;
+          v[i] = (t < p.nt) ? __ldg(reinterpret_cast<const uint4 *>(src + (size_t)t * n * CW))
+                            : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int ci = 0; ci < 4; ci++) {
+          const int cc = 4 * q + ci;
+          const int G = cc / p.g, gi = cc - G * p.g;
+          const int row = gi * p.R + 2 * s;
+          uint32_t w[8];
+#pragma unroll
+          for (int i = 0; i < 8; i++) w[i] = (ci == 0) ? v[i].x : (ci == 1) ? v[i].y : (ci == 2) ? v[i].z : v[i].w;
+          const uint4 re = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410), prmt(w[4], w[5], 0x5410),
+                                      prmt(w[6], w[7], 0x5410));
+          const uint4 im = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632), prmt(w[4], w[5], 0x7632),
+                                      prmt(w[6], w[7], 0x7632));
+          unsigned char *gbase = stage + G * GROUP_BYTES;
+          *reinterpret_cast<uint4 *>(gbase + row * 128 + ((o ^ (row & 7)) << 4)) = re;
+          *reinterpret_cast<uint4 *>(gbase + (row + 1) * 128 + ((o ^ ((row + 1) & 7)) << 4)) = im;
+        }
+      }
+      fence_proxy_async_smem();
+      mbar_arrive(smem_u32(&bar_full[st]));
+    }
+  } else if (lane == 0) {
+    // ------------------------------------------------------------ MMA issuer
+    for (int ch = 0; ch < nchunks; ch++) {
+      const int st = ch % STAGES;
+      if (!mbar_wait(smem_u32(&bar_full[st]), (ch / STAGES) & 1, p.err)) break;
+      tc_fence_after();
+      const uint32_t sa = sbase + st * STAGE_BYTES;
+#pragma unroll
+      for (int G = 0; G < NG; G++) {
+#pragma unroll
+        for (int kk = 0; kk < KC / 16; kk++) {
+          const uint64_t d = desc_sw128(sa + G * GROUP_BYTES + kk * 32);
+          mma_f16(tmem + G * 128, d, d, IDESC, (ch > 0 || kk > 0) ? 1u : 0u);
+        }
+      }
+      mma_commit(smem_u32(&bar_empty[st]));
+    }
+    mma_commit(smem_u32(&bar_done));
+    mbar_wait(smem_u32(&bar_done), 0, p.err);  // issued MMAs drained before TMEM is read or freed
+  }
+
+  // ------------------------------------------------------------ epilogue
+  if (warp < 4) {
+    const bool ok = mbar_wait(smem_u32(&bar_done), 0, p.err);
+    tc_fence_after();
+    if (ok) {
+      const int row = 32 * warp + lane;
+      const int my_gi = row / p.R;
+      const int r = row - my_gi * p.R;
+      const int s1 = r >> 1, part1 = r & 1;
+      const int gi0 = (32 * warp) / p.R;
+      const int col0 = gi0 * p.R;
+      const int clen = p.R > 32 ? p.R : 32;
+      const int j = s1 >> 1, l = s1 & 1;
+      for (int G = 0; G < NG; G++) {
+        const int c = cb + G * p.g + my_gi;
+        for (int pc = 0; pc < clen; pc += 16) {
+          __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skip below
+          const int col = col0 + pc;
+          float v[16], pv[16];
+          tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(G * 128 + col), v);
+#pragma unroll
+          for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
+          if (col < my_gi * p.R || col >= (my_gi + 1) * p.R || s1 >= n) continue;
+          const int s2b = (col - my_gi * p.R) >> 1;
+#pragma unroll
+          for (int qq = 0; qq < 4; qq++) {
+            const int q = qq + 4 * part1;
+            const int s2 = s2b + q;
+            if (s2 >= n) continue;
+            const int k = s2 >> 1, m = s2 & 1;
+            if (j > k || (j == k && !p.autos)) continue;
+            float re, im;
+            if (part1 == 0) {
+              re = v[2 * q] + pv[2 * q + 1];
+              im = pv[2 * q] - v[2 * q + 1];
+            } else {
+              re = pv[2 * q] + v[2 * q + 1];
+              im = v[2 * q] - pv[2 * q + 1];
+            }
+            const int bl = baseline_index(j, k, p.nant);
+            const size_t o = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
+            float2 sm = p.vsum[o], e = p.vcomp[o];
+            two_sum_add(sm.x, e.x, re);
+            two_sum_add(sm.y, e.y, im);
+            p.vsum[o] = sm;
+            p.vcomp[o] = e;
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == NPROD_WARPS) tmem_dealloc(tmem, TMEM_COLS);
+}
+
+}  // namespace tc
+
+// two rows (re, im) per stream, two streams per antenna: 4*nant rows must fit one M=128 tile
+int xstage_tensor_supported(int nant) { return nant >= 1 && 4 * nant <= 128; }
+
+static int g_err_dev = -1;
+static int *g_err = nullptr;
+
+cudaError_t xstage_tensor_error_flag(int **flag) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!g_err || g_err_dev != dev) {
+    cudaError_t e = cudaMalloc(&g_err, sizeof(int));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(g_err, 0, sizeof(int));
+    if (e != cudaSuccess) return e;
+    g_err_dev = dev;
+  }
+  *flag = g_err;
+  return cudaSuccess;
+}
+
+// Reads and clears the device-side timeout flag of the tensor-core X-stage (1 = a wait expired).
+cudaError_t xstage_tensor_take_error(int *flag) {
+  *flag = 0;
+  if (!g_err) return cudaSuccess;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != g_err_dev) return cudaSuccess;
+  cudaError_t e = cudaMemcpy(flag, g_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && *flag) e = cudaMemset(g_err, 0, sizeof(int));
+  return e;
+}
+
+cudaError_t launch_xstage_tensor(const void *chan, int nant, int nchan, int T, int nt, int autos, float2 *vsum,
+                                 float2 *vcomp, cudaStream_t s) {
+  if (nt <= 0) return cudaSuccess;
+  if (!xstage_tensor_supported(nant)) return cudaErrorInvalidValue;
+  tc::Params p;
+  p.chan = (const __half2 *)chan;
+  p.nant = nant;
+  p.nstream = 2 * nant;
+  p.nchan = nchan;
+  p.T = T;
+  p.nt = nt;
+  p.autos = autos;
+  int R = 16;
+  while (R < 2 * p.nstream) R <<= 1;  // 2 rows (re, im) per stream
+  p.R = R;
+  p.g = 128 / R;
+  p.CS = 4 * p.g;
+  if (nchan % p.CS) return cudaErrorInvalidValue;
+  p.vsum = vsum;
+  p.vcomp = vcomp;
+  cudaError_t e = xstage_tensor_error_flag(&p.err);
+  if (e != cudaSuccess) return e;
+  const size_t smem = (size_t)tc::STAGES * tc::STAGE_BYTES + 1024;
+  e = cudaFuncSetAttribute(tc::xstage_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  tc::xstage_tc_kernel<<<nchan / p.CS, tc::NTHREADS, smem, s>>>(p);
+  return cudaGetLastError();
 }
 
 }  // namespace gxc

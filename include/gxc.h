@@ -125,6 +125,19 @@ int gxc_fft_block(const gxc_handle *h);
 gxc_status gxc_enable_stage_timing(gxc_handle *h, int enable);
 gxc_status gxc_stage_times(gxc_handle *h, float *f_ms, float *x_ms, float *total_ms);
 
+/* The X-stage alone, on already-channelised data, as the reference GPU X kernels
+ * take it (gcorr/src/gxkernel.h:86-88, CrossCorrAccumHoriz/CCAH2/CCAH3;
+ * layout gcorr/src/gxkernel.h:30-44): ants is complex float
+ * [nant][2 pols][nfft*fftwidth] with sample f*fftwidth + chan (chan < nchan),
+ * host or device memory.  accum receives complex float [nbl][4][nchan]
+ * (crosses in fxkernel order, then autos when autos != 0), each product
+ * summed over the nfft spectra and divided by nfft as CCAH3 does
+ * (gcorr/src/gxkernel.cu:574-581).  precision: GXC_PRECISION_FP32 or _FP16
+ * (values cast to FP16 unscaled); x_engine: GXC_XENGINE_*.  Synchronous on
+ * `stream`; allocates its scratch with cudaMalloc. */
+gxc_status gxc_xcorr(const float *ants, int nant, int nfft, int nchan, int fftwidth, int precision, int x_engine,
+                     int autos, float *accum, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,108 @@
+"""GPU tests of the X-stage engines through gxc_xcorr.
+
+Known-answer tests follow the reference's X-stage unit tests
+(gcorr/test/unit.cc:73-159): complex data with small integer components
+(uniform in [-5, 5]) so every product and sum is exact in FP32 (and in FP16),
+compared for exact equality with a CPU triple loop (unit.cc:41-71: sum of
+u*conj(v) over the FFTs, divided by nfft).  Same shapes as the reference:
+(nant 3, fftwidth 512, nchan 256, nfft 4), (5, 1024, 1024, 100), (3, 1024, 512, 3000).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import gcorr_gb300 as G
+from gcorr_gb300 import _lib as L
+from gcorr_gb300 import FxKernel, synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+KAT_SHAPES = [(3, 512, 256, 4), (5, 1024, 1024, 100), (3, 1024, 512, 3000)]
+
+
+def cint_data(n, seed=12345):
+    rng = np.random.default_rng(seed)
+    return (rng.integers(-5, 6, n) + 1j * rng.integers(-5, 6, n)).astype(np.complex64)
+
+
+def expected_crosscorraccum(data, nant, nfft, nchan, fftwidth, autos=False):
+    """CPU triple loop of gcorr/test/unit.cc:41-71 (plus autos when asked)."""
+    d = data.reshape(nant, 2, nfft, fftwidth)[..., :nchan].astype(np.complex128)
+    out = []
+    pairs = [(i, j) for i in range(nant - 1) for j in range(i + 1, nant)]
+    if autos:
+        pairs += [(i, i) for i in range(nant)]
+    for i, j in pairs:
+        for pi in range(2):
+            for pj in range(2):
+                out.append((d[i, pi] * np.conj(d[j, pj])).sum(axis=0) / nfft)
+    return np.array(out, dtype=np.complex128).reshape(len(pairs), 4, nchan)
+
+
+def xcorr(data, nant, nfft, nchan, fftwidth, precision, engine, autos=False):
+    nbl = nant * (nant - 1) // 2 + (nant if autos else 0)
+    out = np.zeros((nbl, 4, nchan), dtype=np.complex64)
+    st = G.lib().gxc_xcorr(C.c_void_p(data.ctypes.data), nant, nfft, nchan, fftwidth, precision, engine,
+                           int(autos), C.c_void_p(out.ctypes.data), None)
+    assert st == L.GXC_OK, L.status_name(st)
+    return out
+
+
+ENGINES = [("fp32-cuda-core", L.GXC_PRECISION_FP32, L.GXC_XENGINE_CUDA_CORE),
+           ("fp16-cuda-core", L.GXC_PRECISION_FP16, L.GXC_XENGINE_CUDA_CORE),
+           ("fp16-tensor", L.GXC_PRECISION_FP16, L.GXC_XENGINE_TENSOR)]
+
+
+@pytest.mark.parametrize("shape", KAT_SHAPES)
+@pytest.mark.parametrize("name,prec,eng", ENGINES)
+def test_xstage_known_answer_exact(shape, name, prec, eng):
+    nant, fftwidth, nchan, nfft = shape
+    data = cint_data(2 * nant * fftwidth * nfft)
+    exp = expected_crosscorraccum(data, nant, nfft, nchan, fftwidth).astype(np.complex64)
+    got = xcorr(data, nant, nfft, nchan, fftwidth, prec, eng)
+    assert np.array_equal(got, exp), (name, np.abs(got - exp).max())
+
+
+@pytest.mark.parametrize("nant", [1, 2, 4, 7, 8, 16, 32])
+def test_tensor_vs_cuda_core_with_autos(nant):
+    nchan, fftwidth, nfft = 128, 256, 300
+    rng = np.random.default_rng(nant)
+    n = 2 * nant * fftwidth * nfft
+    data = (rng.normal(size=n) + 1j * rng.normal(size=n)).astype(np.complex64)
+    a = xcorr(data, nant, nfft, nchan, fftwidth, L.GXC_PRECISION_FP16, L.GXC_XENGINE_TENSOR, autos=True)
+    b = xcorr(data, nant, nfft, nchan, fftwidth, L.GXC_PRECISION_FP16, L.GXC_XENGINE_CUDA_CORE, autos=True)
+    ref = expected_crosscorraccum(data, nant, nfft, nchan, fftwidth, autos=True)
+    assert O.rel_rms(a, b) < 1e-5
+    assert O.rel_rms_per_product(a, ref).max() < 2e-3
+
+
+def test_full_pipeline_tensor_fp16_vs_fp64():
+    w = synth.Workload(nant=6, nchan=1024, nfft=100, bw_hz=64e6, rho=0.05, seed=61)
+    d = synth.generate(w)
+    inputs = [x.numpy() for x in d["inputs"]]
+    ref, rc = O.exact_process(O.config_from_workload(w, O.ROT_EXACT, True), inputs, d["poly"], d["fso"])
+    out = {}
+    for eng in ("tensor", "cuda_core"):
+        fx = FxKernel(w.nant, w.nchan, w.nfft, 2, w.lo_hz, w.bw_hz, False, precision="fp16", x_engine=eng,
+                      fft_block=48)
+        fx.setInputData(inputs)
+        fx.setDelays(d["poly"], d["fso"])
+        fx.process()
+        out[eng] = fx.visibilities()
+        assert np.array_equal(fx.baseline_counts(), rc)
+        fx.close()
+    assert O.rel_rms_per_product(out["tensor"], ref).max() < 1e-3
+    assert O.rel_rms(out["tensor"], out["cuda_core"]) < 1e-5
+
+
+def test_tensor_is_default_for_fp16():
+    fx = FxKernel(4, 256, 8, 2, 8.4e9, 32e6, False, precision="fp16")
+    d = synth.random_bytes(synth.Workload(nant=4, nchan=256, nfft=8, bw_hz=32e6))
+    fx.setInputData([x.numpy() for x in d["inputs"]])
+    fx.setDelays(d["poly"], d["fso"])
+    fx.process()
+    v = fx.visibilities()
+    assert np.isfinite(v).all()
+    fx.close()
