@@ -222,15 +222,74 @@ struct FParams {
   int fsub_shift, fsub_mask;  // fsub = 1 << fsub_shift
 };
 
-// One Stockham pass (radix R, span P) reading smem, leaving results in u.
-template <int N, int R, int P>
-__device__ __forceinline__ void pass_load(const float2 *buf, const float2 *__restrict__ tw, float2 (&u)[16], int tid) {
+// W32^k = exp(-2 pi i k / 32), k < 16
+__device__ constexpr float kC32[16] = {1.0f, 0.98078528040323044913f, 0.92387953251128675613f,
+                                       0.83146961230254523708f, 0.70710678118654752440f, 0.55557023301960222474f,
+                                       0.38268343236508977173f, 0.19509032201612826785f, 0.0f,
+                                       -0.19509032201612826785f, -0.38268343236508977173f, -0.55557023301960222474f,
+                                       -0.70710678118654752440f, -0.83146961230254523708f, -0.92387953251128675613f,
+                                       -0.98078528040323044913f};
+__device__ constexpr float kS32[16] = {0.0f, 0.19509032201612826785f, 0.38268343236508977173f,
+                                       0.55557023301960222474f, 0.70710678118654752440f, 0.83146961230254523708f,
+                                       0.92387953251128675613f, 0.98078528040323044913f, 1.0f,
+                                       0.98078528040323044913f, 0.92387953251128675613f, 0.83146961230254523708f,
+                                       0.70710678118654752440f, 0.55557023301960222474f, 0.38268343236508977173f,
+                                       0.19509032201612826785f};
+// 32 = 16 (n1) x 2 (n2): n = 2 n1 + n2, k = k1 + 16 k2.
+template <> __device__ __forceinline__ void dft<32>(float2 *u) {
+  float2 a[16], b[16];
 #pragma unroll
-  for (int q = 0; q < 16 / R; q++) {
-    const int iv = tid + q * (N / 16);
+  for (int i = 0; i < 16; i++) {
+    a[i] = u[2 * i];
+    b[i] = u[2 * i + 1];
+  }
+  dft<16>(a);
+  dft<16>(b);
+#pragma unroll
+  for (int k = 1; k < 16; k++) b[k] = cmul(b[k], make_float2(kC32[k], -kS32[k]));
+#pragma unroll
+  for (int k = 0; k < 16; k++) {
+    u[k] = cadd(a[k], b[k]);
+    u[k + 16] = csub(a[k], b[k]);
+  }
+}
+
+// Radix schedule: 2 or 3 in-register passes with radices <= 32 (product = 2^L).
+// A CTA transforms one pol of one FFT window; each of its F/32 threads holds
+// 32 complex values per pass, and two CTAs share an SM.
+template <int L>
+struct FPlan {
+  static constexpr int N = 1 << L;
+  static constexpr int POLS = 1;
+  static constexpr int NTW = N / 32;                  // threads with FFT work
+  static constexpr int NT = NTW < 32 ? 32 : NTW;      // threads launched
+  static constexpr int R0 = L == 8 ? 16 : L == 9 ? 32 : L == 10 ? 32 : L == 11 ? 8 : L == 12 ? 16 : L == 13 ? 32 : 16;
+  static constexpr int R1 = L == 8 ? 16 : L == 9 ? 16 : L == 10 ? 32 : L == 14 ? 32 : 16;
+  static constexpr int R2 = L <= 10 ? 1 : (L == 14 ? 32 : 16);
+  static constexpr int PAD0 = R0;                     // smem padding after the first pass (stride-R0 stores)
+  static constexpr int PADN = N + N / 8;              // padded complex slots (covers PAD0 >= 8 and 32)
+  static constexpr int MINB = (L >= 14) ? 1 : 2;      // CTAs per SM (F = 16384 fills the shared memory)
+  static_assert(R0 * R1 * R2 == N, "radix schedule");
+};
+
+// Shared-memory padding: one slot per D keeps strided stores conflict-free.
+template <int D>
+__device__ __forceinline__ int padi(int i) { return i + i / D; }
+
+// Stockham pass (radix R, span P): loads 32/R butterflies per thread from smem,
+// applies the twiddles W_{PR}^{rk} and the radix-R DFT in registers.
+template <int N, int R, int P, int NTW, int POLS, int PAD>
+__device__ __forceinline__ void pass_load(const float2 *buf, const float2 *__restrict__ tw, float2 (&u)[32], int tid) {
+  constexpr int NB = N / R;  // butterflies per pol
+#pragma unroll
+  for (int q = 0; q < 32 / R; q++) {
+    const int vb = tid + q * NTW;
+    const int pol = (POLS == 2) ? vb / NB : 0;
+    const int iv = vb & (NB - 1);
     const int k = iv & (P - 1);
+    const float2 *b = buf + pol * (N + N / 8);
 #pragma unroll
-    for (int r = 0; r < R; r++) u[q * R + r] = buf[pidx(iv + r * (N / R))];
+    for (int r = 0; r < R; r++) u[q * R + r] = b[padi<PAD>(iv + r * NB)];
     if (P > 1) {
 #pragma unroll
       for (int r = 1; r < R; r++) u[q * R + r] = cmul(u[q * R + r], __ldg(&tw[r * k * (N / (P * R))]));
@@ -239,60 +298,45 @@ __device__ __forceinline__ void pass_load(const float2 *buf, const float2 *__res
   }
 }
 
-template <int N, int R, int P>
-__device__ __forceinline__ void pass_store(float2 *buf, const float2 (&u)[16], int tid) {
+template <int N, int R, int P, int NTW, int POLS, int PAD>
+__device__ __forceinline__ void pass_store(float2 *buf, const float2 (&u)[32], int tid) {
+  constexpr int NB = N / R;
 #pragma unroll
-  for (int q = 0; q < 16 / R; q++) {
-    const int iv = tid + q * (N / 16);
+  for (int q = 0; q < 32 / R; q++) {
+    const int vb = tid + q * NTW;
+    const int pol = (POLS == 2) ? vb / NB : 0;
+    const int iv = vb & (NB - 1);
     const int k = iv & (P - 1);
     const int j = (iv - k) * R + k;
+    float2 *b = buf + pol * (N + N / 8);
 #pragma unroll
-    for (int r = 0; r < R; r++) buf[pidx(j + r * P)] = u[q * R + r];
+    for (int r = 0; r < R; r++) b[padi<PAD>(j + r * P)] = u[q * R + r];
   }
 }
 
-// Middle radix-16 passes, P = P0 .. N/256 (the last pass is handled by the caller).
-template <int N, int P>
-struct MidPasses {
-  __device__ __forceinline__ static void run(float2 *buf, const float2 *__restrict__ tw, float2 (&u)[16], int tid,
-                                             bool active) {
-    if constexpr (P * 16 < N) {
-      if (active) pass_load<N, 16, P>(buf, tw, u, tid);
-      __syncthreads();
-      if (active) pass_store<N, 16, P>(buf, u, tid);
-      __syncthreads();
-      MidPasses<N, P * 16>::run(buf, tw, u, tid, active);
-    }
-  }
-};
-
-template <int L>
-struct FftPlan {
-  static constexpr int N = 1 << L;
-  static constexpr int R0 = (L % 4) ? (1 << (L % 4)) : 16;
-  static constexpr int NV = N / 16;                 // threads doing FFT work
-  static constexpr int NT = NV < 32 ? 32 : NV;      // threads launched
-};
-
 template <int L, typename OutT, bool CPLX>
-__global__ void __launch_bounds__(FftPlan<L>::NT) fstage_kernel(FParams prm) {
-  using Plan = FftPlan<L>;
-  constexpr int N = Plan::N;
-  constexpr int R0 = Plan::R0;
-  constexpr int NV = Plan::NV;
-  constexpr int NT = Plan::NT;
+__global__ void __launch_bounds__(FPlan<L>::NT, FPlan<L>::MINB) fstage_kernel(FParams prm) {
+  using Pl = FPlan<L>;
+  constexpr int N = Pl::N, NT = Pl::NT, NTW = Pl::NTW, POLS = Pl::POLS;
+  constexpr int R0 = Pl::R0, R1 = Pl::R1, R2 = Pl::R2, PAD0 = Pl::PAD0;
+  constexpr int RL = (R2 > 1) ? R2 : R1;              // radix of the last pass
+  constexpr int PL = N / RL;                          // its span
+  constexpr int STAGE_BYTES = CPLX ? 4 * N + 32 : N / 2 + 32;
   const Job &job = prm.job;
   extern __shared__ float2 smem[];
-  float2 *buf = smem;                          // N + N/16 (padded)
-  float2 *tsub = buf + N + N / 16;             // fringe rotator, fine part  [substride]
-  float2 *tstep = tsub + job.substride;        // fringe rotator, coarse part [stride]
-  float2 *fsubt = tstep + job.stride;          // frac-delay, fine part [fsub]
-  float2 *fstept = fsubt + job.fsub;           // frac-delay, coarse part [fstride]
+  float2 *buf = smem;                                 // POLS x (N + N/16)
+  float2 *tsub = buf + POLS * Pl::PADN;               // fringe rotator, fine part  [substride]
+  float2 *tstep = tsub + job.substride;               // fringe rotator, coarse part [stride]
+  float2 *fsubt = tstep + job.stride;                 // frac-delay, fine part [fsub]
+  float2 *fstept = fsubt + job.fsub;                  // frac-delay, coarse part [fstride]
+  unsigned char *stage = reinterpret_cast<unsigned char *>(fstept + job.fstride);  // packed input window
   __shared__ Geom g;
   __shared__ float cst[4];
+  __shared__ long long stage_base;
 
   const int tl = blockIdx.x;
   const int ant = blockIdx.y;
+  const int cpol = blockIdx.z;  // the pol this CTA transforms
   const int t = prm.t0 + tl;
   const int tid = threadIdx.x;
   const int nstreams = 2 * job.nant;
@@ -310,7 +354,7 @@ __global__ void __launch_bounds__(FftPlan<L>::NT) fstage_kernel(FParams prm) {
       if (job.fractional_lo) c0 += (job.lo_hz - trunc(job.lo_hz)) * (double)intdelay;
       c0 -= floor(c0);
       const double c1 = g.a * job.lo_hz / (double)job.F;  // turns per sample
-      // coarse step: the reference advances the step table by `stride` samples
+      // coarse step: the reference advances its step table by `stride` samples
       // per entry (fxkernel.cpp:112) while applying it every `substride` samples;
       // FXKERNEL mode keeps that, EXACT uses the true step.
       const double stepmul = (job.rotator == GXC_ROTATOR_FXKERNEL) ? (double)job.stride : (double)job.substride;
@@ -319,6 +363,8 @@ __global__ void __launch_bounds__(FftPlan<L>::NT) fstage_kernel(FParams prm) {
       cst[2] = (float)(c1 * stepmul);
       // fractional-sample correction: exp(+2 pi i c bw/nchan frac) (fxkernel.cpp:171-175,600-630)
       cst[3] = (float)(job.bw_hz / (double)nchan * g.frac);  // turns per channel
+      const long long first = CPLX ? 4LL * g.offset : ((long long)g.offset >> 1);
+      stage_base = first & ~15LL;
     }
   }
   __syncthreads();
@@ -326,66 +372,76 @@ __global__ void __launch_bounds__(FftPlan<L>::NT) fstage_kernel(FParams prm) {
   if (!g.valid) {
     // flagged: the X-stage sums zeros, the baseline counts exclude this FFT
     const OutT z = to_out<OutT>(make_float2(0.f, 0.f), 1.f);
-    for (int p = 0; p < 2; p++) {
-      const int s = 2 * ant + p;
-      for (int c = tid; c < nchan; c += NT) {
-        const size_t o = (((size_t)(c >> 4) * prm.T + tl) * nstreams + s) * CW + (c & 15);
-        chan[o] = z;
-      }
+    const int s = 2 * ant + cpol;
+    for (int c = tid; c < nchan; c += NT) {
+      const size_t o = (((size_t)(c >> 4) * prm.T + tl) * nstreams + s) * CW + (c & 15);
+      chan[o] = z;
     }
     return;
   }
 
   {
+    // stage the packed window with 16-byte loads (bounds: the buffer holds
+    // (nfft+1)*F samples and offset <= (nfft-1)*F, so the window plus the
+    // 16-byte rounding stays inside it)
+    const uint4 *src = reinterpret_cast<const uint4 *>(job.inputs[ant] + stage_base);
+    const long long last = CPLX ? 4LL * (g.offset + N) : (((long long)g.offset + N + 1) >> 1);
+    const int nvec = (int)((last - stage_base + 15) >> 4);
+    uint4 *dst = reinterpret_cast<uint4 *>(stage);
+    for (int i = tid; i < nvec; i += NT) dst[i] = __ldg(&src[i]);
     const float c0 = cst[0], c1 = cst[1], cstep = cst[2], cf = cst[3];
     for (int k = tid; k < job.substride; k += NT) {
-      float s, c;
-      sincospif(-2.0f * fmaf((float)k, c1, c0), &s, &c);
-      tsub[k] = make_float2(c, s);
+      float sn, cs;
+      sincospif(-2.0f * fmaf((float)k, c1, c0), &sn, &cs);
+      tsub[k] = make_float2(cs, sn);
     }
     for (int i = tid; i < job.stride; i += NT) {
-      float s, c;
-      sincospif(-2.0f * ((float)i * cstep), &s, &c);
-      tstep[i] = make_float2(c, s);
+      float sn, cs;
+      sincospif(-2.0f * ((float)i * cstep), &sn, &cs);
+      tstep[i] = make_float2(cs, sn);
     }
     for (int k = tid; k < job.fsub; k += NT) {
-      float s, c;
-      sincospif(2.0f * ((float)k * cf), &s, &c);
-      fsubt[k] = make_float2(c, s);
+      float sn, cs;
+      sincospif(2.0f * ((float)k * cf), &sn, &cs);
+      fsubt[k] = make_float2(cs, sn);
     }
     for (int i = tid; i < job.fstride; i += NT) {
-      float s, c;
-      sincospif(2.0f * ((float)(i << prm.fsub_shift) * cf), &s, &c);
-      fstept[i] = make_float2(c, s);
+      float sn, cs;
+      sincospif(2.0f * ((float)(i << prm.fsub_shift) * cf), &sn, &cs);
+      fstept[i] = make_float2(cs, sn);
     }
   }
   __syncthreads();
 
-  const bool active = tid < NV;
-  const uint8_t *in = job.inputs[ant];
+  const bool active = tid < NTW;
   const long long off = g.offset;
+  const int sbase = (int)(CPLX ? (4LL * off - stage_base) : ((off >> 1) - stage_base));
 
-  for (int pol = 0; pol < 2; pol++) {
-    float2 u[16];
-    // ---- first pass: decode + rotate straight from the packed input
+  {
+    const int pass_pol = cpol;
+    float2 u[32];
+    // ---- first pass (P = 1): decode + rotate from the staged window
     if (active) {
+      constexpr int NB = N / R0;
 #pragma unroll
-      for (int q = 0; q < 16 / R0; q++) {
-        const int iv = tid + q * NV;
+      for (int q = 0; q < 32 / R0; q++) {
+        const int vb = tid + q * NTW;
+        const int pol = (POLS == 2) ? vb / NB : pass_pol;
+        const int iv = vb & (NB - 1);
 #pragma unroll
         for (int r = 0; r < R0; r++) {
-          const int n = iv + r * (N / R0);
+          const int n = iv + r * NB;
           const float2 rot = cmul(tsub[n & prm.sub_mask], tstep[n >> prm.sub_shift]);
-          const long long m = off + n;
           float2 x;
           if constexpr (CPLX) {
             // int8 (A.re, A.im, B.re, B.im) per time sample
-            const char2 v = __ldg(reinterpret_cast<const char2 *>(in + m * 4 + 2 * pol));
+            const char2 v = *reinterpret_cast<const char2 *>(stage + sbase + 4 * n + 2 * pol);
             x = cmul(make_float2((float)v.x, (float)v.y), rot);
           } else {
             // 2-bit: byte m/2 holds A_m', B_m', A_m'+1, B_m'+1 (fxkernel.cpp:443-476)
-            const int byte = __ldg(in + (m >> 1));
-            const int code = (byte >> (2 * (2 * (int)(m & 1) + pol))) & 3;
+            const int m = (int)(off & 1) + n;  // sample index relative to byte (off >> 1)
+            const int byte = stage[sbase + (m >> 1)];
+            const int code = (byte >> (2 * (2 * (m & 1) + pol))) & 3;
             const float v = level2bit(code);
             x = make_float2(v * rot.x, v * rot.y);
           }
@@ -394,22 +450,33 @@ __global__ void __launch_bounds__(FftPlan<L>::NT) fstage_kernel(FParams prm) {
         dft<R0>(&u[q * R0]);
       }
     }
-    __syncthreads();  // previous pol's last pass has finished reading buf
-    if (active) pass_store<N, R0, 1>(buf, u, tid);
+    if (active) pass_store<N, R0, 1, NTW, POLS, PAD0>(buf, u, tid);
     __syncthreads();
-    MidPasses<N, R0>::run(buf, prm.tw, u, tid, active);
-    // ---- last radix-16 pass: outputs c = tid + r*N/16 go straight to global
+    if constexpr (R2 > 1) {
+      if (active) pass_load<N, R1, R0, NTW, POLS, PAD0>(buf, prm.tw, u, tid);
+      __syncthreads();
+      if (active) pass_store<N, R1, R0, NTW, POLS, 32>(buf, u, tid);
+      __syncthreads();
+    }
+    // ---- last pass: outputs c = iv + r*N/RL go straight to global
     if (active) {
-      pass_load<N, 16, N / 16>(buf, prm.tw, u, tid);
-      const int s = 2 * ant + pol;
+      pass_load<N, RL, PL, NTW, POLS, (R2 > 1 ? 32 : PAD0)>(buf, prm.tw, u, tid);
+      constexpr int NB = N / RL;
 #pragma unroll
-      for (int r = 0; r < 16; r++) {
-        const int c = tid + r * (N / 16);
-        if (c < nchan) {
-          const float2 fr = cmul(fsubt[c & prm.fsub_mask], fstept[c >> prm.fsub_shift]);
-          const float2 y = cmul(u[r], fr);
-          const size_t o = (((size_t)(c >> 4) * prm.T + tl) * nstreams + s) * CW + (c & 15);
-          chan[o] = to_out<OutT>(y, prm.out_scale);
+      for (int q = 0; q < 32 / RL; q++) {
+        const int vb = tid + q * NTW;
+        const int pol = (POLS == 2) ? vb / NB : pass_pol;
+        const int iv = vb & (NB - 1);
+        const int s = 2 * ant + pol;
+#pragma unroll
+        for (int r = 0; r < RL; r++) {
+          const int c = iv + r * NB;
+          if (c < nchan) {
+            const float2 fr = cmul(fsubt[c & prm.fsub_mask], fstept[c >> prm.fsub_shift]);
+            const float2 y = cmul(u[q * RL + r], fr);
+            const size_t o = (((size_t)(c >> 4) * prm.T + tl) * nstreams + s) * CW + (c & 15);
+            chan[o] = to_out<OutT>(y, prm.out_scale);
+          }
         }
       }
     }
@@ -418,15 +485,16 @@ __global__ void __launch_bounds__(FftPlan<L>::NT) fstage_kernel(FParams prm) {
 
 template <int L, typename OutT, bool CPLX>
 static cudaError_t launch_fstage_t(const FParams &prm, int nt, cudaStream_t s) {
-  using Plan = FftPlan<L>;
+  using Pl = FPlan<L>;
   const Job &job = prm.job;
-  const size_t smem = sizeof(float2) * ((size_t)Plan::N + Plan::N / 16 + job.substride + job.stride + job.fsub +
-                                        job.fstride);
+  const size_t stage_bytes = CPLX ? 4 * (size_t)Pl::N + 32 : (size_t)Pl::N / 2 + 32;
+  const size_t smem = sizeof(float2) * ((size_t)Pl::POLS * Pl::PADN + job.substride + job.stride + job.fsub +
+                                        job.fstride) + ((stage_bytes + 15) & ~(size_t)15);
   auto kern = fstage_kernel<L, OutT, CPLX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)nt, (unsigned)job.nant);
-  kern<<<grid, Plan::NT, smem, s>>>(prm);
+  dim3 grid((unsigned)nt, (unsigned)job.nant, 2u);
+  kern<<<grid, Pl::NT, smem, s>>>(prm);
   return cudaGetLastError();
 }
 
