@@ -26,7 +26,7 @@ EXPORTS = [
     "gxc_status_string", "gxc_create", "gxc_destroy", "gxc_set_input", "gxc_set_delays", "gxc_process",
     "gxc_sync", "gxc_accumulate", "gxc_get_visibilities", "gxc_device_visibilities", "gxc_get_baseline_counts",
     "gxc_get_valid_flags", "gxc_last_error", "gxc_last_launch_count", "gxc_fft_block", "gxc_enable_stage_timing",
-    "gxc_stage_times", "gxc_xcorr"
+    "gxc_stage_times", "gxc_xcorr", "gxc_xcorr_noalloc",
 ]
 
 
@@ -102,6 +102,8 @@ def lib():
         l.gxc_stage_times.restype = C.c_int
         l.gxc_xcorr.argtypes = [V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, V, V]
         l.gxc_xcorr.restype = C.c_int
+        l.gxc_xcorr_noalloc.argtypes = [V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, V, V]
+        l.gxc_xcorr_noalloc.restype = C.c_int
         _lib = l
     return _lib
 

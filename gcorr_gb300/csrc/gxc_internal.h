@@ -56,6 +56,10 @@ int fstage_supported(int F);
 cudaError_t launch_xstage_cuda_core(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,
                                     float2 *vsum, float2 *vcomp, cudaStream_t s);
 
+cudaError_t launch_xstage_cuda_core_pairs(const void *chan, int chan_type, int nant, int nchan, int T, int nt,
+                                          int autos, const int2 *pairs, float2 *vsum, float2 *vcomp,
+                                          cudaStream_t s);
+
 // xstage_tc.cu: tcgen05 tensor-core X-stage over FP16 channelised data.
 cudaError_t launch_xstage_tensor(const void *chan, int nant, int nchan, int T, int nt, int autos, float2 *vsum,
                                  float2 *vcomp, cudaStream_t s);

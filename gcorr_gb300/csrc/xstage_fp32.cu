@@ -179,4 +179,38 @@ cudaError_t launch_xstage_cuda_core(const void *chan, int chan_type, int nant, i
   return cudaGetLastError();
 }
 
+// Same launch with a caller-provided tile-pair table (J <= K over ceil(nant/2)
+// antenna tiles, J-major), for callers that keep the table in their own memory.
+cudaError_t launch_xstage_cuda_core_pairs(const void *chan, int chan_type, int nant, int nchan, int T, int nt,
+                                          int autos, const int2 *pairs, float2 *vsum, float2 *vcomp,
+                                          cudaStream_t s) {
+  if (nt <= 0) return cudaSuccess;
+  const int nat = (nant + 1) / 2;
+  const int npairs = nat * (nat + 1) / 2;
+  const int nstream = 2 * nant;
+  const size_t esz = chan_type == CHAN_F32 ? sizeof(float2) : sizeof(__half2);
+  const int pairs_per_cta = npairs < 64 ? npairs : 64;
+  const int threads = pairs_per_cta * CW;
+  int TT = (int)(65536 / ((size_t)nstream * CW * esz));
+  if (TT < 1) TT = 1;
+  if (TT > 32) TT = 32;
+  const size_t smem = (size_t)TT * nstream * CW * esz;
+  dim3 grid((unsigned)((npairs + pairs_per_cta - 1) / pairs_per_cta), (unsigned)((nchan + CW - 1) / CW));
+  cudaError_t e;
+  if (chan_type == CHAN_F32) {
+    auto k = xstage_cc_kernel<float2>;
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, threads, smem, s>>>((const float2 *)chan, nant, nchan, T, nt, autos, pairs, npairs, pairs_per_cta, TT,
+                                   vsum, vcomp);
+  } else {
+    auto k = xstage_cc_kernel<__half2>;
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, threads, smem, s>>>((const __half2 *)chan, nant, nchan, T, nt, autos, pairs, npairs, pairs_per_cta, TT,
+                                   vsum, vcomp);
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace gxc

@@ -138,6 +138,23 @@ gxc_status gxc_stage_times(gxc_handle *h, float *f_ms, float *x_ms, float *total
 gxc_status gxc_xcorr(const float *ants, int nant, int nfft, int nchan, int fftwidth, int precision, int x_engine,
                      int autos, float *accum, void *stream);
 
+/* gxc_xcorr for callers that cannot allocate device memory.  No counterpart in
+ * the reference: it exists for code where cudaMalloc is off limits (a host
+ * callback or real-time ingest thread that must not block on the allocator,
+ * which can synchronise the device; a process whose GPU memory budget belongs
+ * to a framework that owns every allocation).  Same arguments and results as
+ * gxc_xcorr with the CUDA-core engine, but ants and accum must already be
+ * device memory, and the scratch lives in one fixed array of
+ * GXC_XCORR_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library
+ * until the process exits.  Problems whose accumulators (nbl*4*nchan complex
+ * float, twice) plus one FFT of channelised data do not fit are rejected with
+ * GXC_ERR_INVALID_ARGUMENT.  The call only enqueues work on `stream`.  The
+ * first call on a device looks up the array's device address (do it before
+ * any stream capture); calls that overlap on the GPU share the array and race. */
+#define GXC_XCORR_NOALLOC_SCRATCH_BYTES (16u << 20)
+gxc_status gxc_xcorr_noalloc(const float *ants, int nant, int nfft, int nchan, int fftwidth, int precision,
+                             int autos, float *accum, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
