@@ -194,10 +194,6 @@ template <> __device__ __forceinline__ void dft<16>(float2 *u) {
   for (int q = 0; q < 16; q++) u[q] = y[q];
 }
 
-// Shared-memory index padding: one float2 of padding per 16 keeps the
-// stride-R writes of the early Stockham passes free of bank conflicts.
-__device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
-
 __device__ __forceinline__ float level2bit(int code) {
   // fxkernel.cpp:17-18: {-HiMag, -1, 1, HiMag}, HiMag = 3.3359
   const float mag = (code == 0 || code == 3) ? 3.3359f : 1.0f;
@@ -254,93 +250,77 @@ template <> __device__ __forceinline__ void dft<32>(float2 *u) {
   }
 }
 
-// Radix schedule: 2 or 3 in-register passes with radices <= 32 (product = 2^L).
+constexpr int hibit(int r) { return r >= 16 ? 16 : r >= 8 ? 8 : r >= 4 ? 4 : r >= 2 ? 2 : 1; }
+constexpr int log2c(int x) { return x <= 1 ? 0 : 1 + log2c(x / 2); }
+
+// Radix schedule and compile-time table splits for FFT length 2^L.
 // A CTA transforms one pol of one FFT window; each of its F/32 threads holds
-// 32 complex values per pass, and two CTAs share an SM.
-template <int L>
+// 32 complex values per pass (2 or 3 passes, radices <= 32); two CTAs share an SM.
+template <int L, bool CPLX>
 struct FPlan {
   static constexpr int N = 1 << L;
-  static constexpr int POLS = 1;
   static constexpr int NTW = N / 32;                  // threads with FFT work
   static constexpr int NT = NTW < 32 ? 32 : NTW;      // threads launched
   static constexpr int R0 = L == 8 ? 16 : L == 9 ? 32 : L == 10 ? 32 : L == 11 ? 8 : L == 12 ? 16 : L == 13 ? 32 : 16;
   static constexpr int R1 = L == 8 ? 16 : L == 9 ? 16 : L == 10 ? 32 : L == 14 ? 32 : 16;
   static constexpr int R2 = L <= 10 ? 1 : (L == 14 ? 32 : 16);
-  static constexpr int PAD0 = R0;                     // smem padding after the first pass (stride-R0 stores)
-  static constexpr int PADN = N + N / 8;              // padded complex slots (covers PAD0 >= 8 and 32)
+  static constexpr int RL = R2 > 1 ? R2 : R1;         // radix of the last pass
+  static constexpr int PAD = R0;                      // one smem slot of padding per R0 (conflict-free strided stores)
+  static constexpr int PADN = N + N / R0;
   static constexpr int MINB = (L >= 14) ? 1 : 2;      // CTAs per SM (F = 16384 fills the shared memory)
+  // table splits, fxkernel.cpp:57-64 (stride = sqrt(nchan) for square nchan; 2^floor(log2(nchan)/2) otherwise)
+  static constexpr int NCHAN = CPLX ? N : N / 2;
+  static constexpr int STRIDE = 1 << (log2c(NCHAN) / 2);
+  static constexpr int SUB = N / STRIDE;              // fringe sub-table (substride)
+  static constexpr int FSUB = NCHAN / STRIDE;         // frac-delay sub-table
   static_assert(R0 * R1 * R2 == N, "radix schedule");
 };
 
-// Shared-memory padding: one slot per D keeps strided stores conflict-free.
-template <int D>
-__device__ __forceinline__ int padi(int i) { return i + i / D; }
-
-// Stockham pass (radix R, span P): loads 32/R butterflies per thread from smem,
-// applies the twiddles W_{PR}^{rk} and the radix-R DFT in registers.
-template <int N, int R, int P, int NTW, int POLS, int PAD>
-__device__ __forceinline__ void pass_load(const float2 *buf, const float2 *__restrict__ tw, float2 (&u)[32], int tid) {
-  constexpr int NB = N / R;  // butterflies per pol
+// u[q*R + r] *= W_N^{r*k*S}, S = N/(P*R): exact table loads at powers of two,
+// the rest as products of at most four of them.
+template <int N, int R, int P>
+__device__ __forceinline__ void twiddle(float2 *u, int k, const float2 *__restrict__ tw) {
+  constexpr int S = N / (P * R);
+  float2 w[R < 16 ? R : 16];
 #pragma unroll
-  for (int q = 0; q < 32 / R; q++) {
-    const int vb = tid + q * NTW;
-    const int pol = (POLS == 2) ? vb / NB : 0;
-    const int iv = vb & (NB - 1);
-    const int k = iv & (P - 1);
-    const float2 *b = buf + pol * (N + N / 8);
-#pragma unroll
-    for (int r = 0; r < R; r++) u[q * R + r] = b[padi<PAD>(iv + r * NB)];
-    if (P > 1) {
-#pragma unroll
-      for (int r = 1; r < R; r++) u[q * R + r] = cmul(u[q * R + r], __ldg(&tw[r * k * (N / (P * R))]));
-    }
-    dft<R>(&u[q * R]);
+  for (int r = 1; r < R && r < 16; r++) {
+    if ((r & (r - 1)) == 0) w[r] = __ldg(&tw[r * k * S]);
+    else w[r] = cmul(w[hibit(r)], w[r - hibit(r)]);
+    u[r] = cmul(u[r], w[r]);
   }
-}
-
-template <int N, int R, int P, int NTW, int POLS, int PAD>
-__device__ __forceinline__ void pass_store(float2 *buf, const float2 (&u)[32], int tid) {
-  constexpr int NB = N / R;
+  if constexpr (R == 32) {
+    const float2 w16 = __ldg(&tw[16 * k * S]);
+    u[16] = cmul(u[16], w16);
 #pragma unroll
-  for (int q = 0; q < 32 / R; q++) {
-    const int vb = tid + q * NTW;
-    const int pol = (POLS == 2) ? vb / NB : 0;
-    const int iv = vb & (NB - 1);
-    const int k = iv & (P - 1);
-    const int j = (iv - k) * R + k;
-    float2 *b = buf + pol * (N + N / 8);
-#pragma unroll
-    for (int r = 0; r < R; r++) b[padi<PAD>(j + r * P)] = u[q * R + r];
+    for (int r = 17; r < 32; r++) u[r] = cmul(u[r], cmul(w16, w[r - 16]));
   }
 }
 
 template <int L, typename OutT, bool CPLX>
-__global__ void __launch_bounds__(FPlan<L>::NT, FPlan<L>::MINB) fstage_kernel(FParams prm) {
-  using Pl = FPlan<L>;
-  constexpr int N = Pl::N, NT = Pl::NT, NTW = Pl::NTW, POLS = Pl::POLS;
-  constexpr int R0 = Pl::R0, R1 = Pl::R1, R2 = Pl::R2, PAD0 = Pl::PAD0;
-  constexpr int RL = (R2 > 1) ? R2 : R1;              // radix of the last pass
-  constexpr int PL = N / RL;                          // its span
-  constexpr int STAGE_BYTES = CPLX ? 4 * N + 32 : N / 2 + 32;
+__global__ void __launch_bounds__(FPlan<L, CPLX>::NT, FPlan<L, CPLX>::MINB) fstage_kernel(FParams prm) {
+  using Pl = FPlan<L, CPLX>;
+  constexpr int N = Pl::N, NT = Pl::NT, NTW = Pl::NTW;
+  constexpr int R0 = Pl::R0, R1 = Pl::R1, R2 = Pl::R2, RL = Pl::RL, PAD = Pl::PAD;
+  constexpr int SUB = Pl::SUB, STRIDE = Pl::STRIDE, FSUB = Pl::FSUB, NCHAN = Pl::NCHAN;
   const Job &job = prm.job;
   extern __shared__ float2 smem[];
-  float2 *buf = smem;                                 // POLS x (N + N/16)
-  float2 *tsub = buf + POLS * Pl::PADN;               // fringe rotator, fine part  [substride]
-  float2 *tstep = tsub + job.substride;               // fringe rotator, coarse part [stride]
-  float2 *fsubt = tstep + job.stride;                 // frac-delay, fine part [fsub]
-  float2 *fstept = fsubt + job.fsub;                  // frac-delay, coarse part [fstride]
-  unsigned char *stage = reinterpret_cast<unsigned char *>(fstept + job.fstride);  // packed input window
+  float2 *buf = smem;                     // N + N/R0 (padded)
+  float2 *tsub = buf + Pl::PADN;          // fringe rotator, fine part  [SUB]
+  float2 *tstep = tsub + SUB;             // fringe rotator, coarse part [STRIDE]
+  float2 *fsubt = tstep + STRIDE;         // frac-delay, fine part [FSUB]
+  float2 *fstept = fsubt + FSUB;          // frac-delay, coarse part [STRIDE]
+  unsigned char *stage = reinterpret_cast<unsigned char *>(fstept + STRIDE);  // packed input window
   __shared__ Geom g;
   __shared__ float cst[4];
   __shared__ long long stage_base;
 
   const int tl = blockIdx.x;
   const int ant = blockIdx.y;
-  const int cpol = blockIdx.z;  // the pol this CTA transforms
+  const int pol = blockIdx.z;  // the pol this CTA transforms
   const int t = prm.t0 + tl;
   const int tid = threadIdx.x;
   const int nstreams = 2 * job.nant;
-  const int nchan = job.nchan;
+  const int s = 2 * ant + pol;
   OutT *chan = reinterpret_cast<OutT *>(prm.chan);
 
   if (tid == 0) {
@@ -353,30 +333,30 @@ __global__ void __launch_bounds__(FPlan<L>::NT, FPlan<L>::MINB) fstage_kernel(FP
       double c0 = br * job.lo_hz;
       if (job.fractional_lo) c0 += (job.lo_hz - trunc(job.lo_hz)) * (double)intdelay;
       c0 -= floor(c0);
-      const double c1 = g.a * job.lo_hz / (double)job.F;  // turns per sample
+      const double c1 = g.a * job.lo_hz / (double)N;  // turns per sample
       // coarse step: the reference advances its step table by `stride` samples
       // per entry (fxkernel.cpp:112) while applying it every `substride` samples;
       // FXKERNEL mode keeps that, EXACT uses the true step.
-      const double stepmul = (job.rotator == GXC_ROTATOR_FXKERNEL) ? (double)job.stride : (double)job.substride;
+      const double stepmul = (job.rotator == GXC_ROTATOR_FXKERNEL) ? (double)STRIDE : (double)SUB;
       cst[0] = (float)c0;
       cst[1] = (float)c1;
       cst[2] = (float)(c1 * stepmul);
       // fractional-sample correction: exp(+2 pi i c bw/nchan frac) (fxkernel.cpp:171-175,600-630)
-      cst[3] = (float)(job.bw_hz / (double)nchan * g.frac);  // turns per channel
+      cst[3] = (float)(job.bw_hz / (double)NCHAN * g.frac);  // turns per channel
       const long long first = CPLX ? 4LL * g.offset : ((long long)g.offset >> 1);
       stage_base = first & ~15LL;
     }
   }
   __syncthreads();
 
+  // channelised layout [ctile][t][stream][16]: element (c, s) of this FFT
+  OutT *out0 = chan + ((size_t)tl * nstreams + s) * CW;
+  const size_t ctile_stride = (size_t)prm.T * nstreams * CW;
+
   if (!g.valid) {
     // flagged: the X-stage sums zeros, the baseline counts exclude this FFT
     const OutT z = to_out<OutT>(make_float2(0.f, 0.f), 1.f);
-    const int s = 2 * ant + cpol;
-    for (int c = tid; c < nchan; c += NT) {
-      const size_t o = (((size_t)(c >> 4) * prm.T + tl) * nstreams + s) * CW + (c & 15);
-      chan[o] = z;
-    }
+    for (int c = tid; c < NCHAN; c += NT) out0[(size_t)(c >> 4) * ctile_stride + (c & 15)] = z;
     return;
   }
 
@@ -390,94 +370,126 @@ __global__ void __launch_bounds__(FPlan<L>::NT, FPlan<L>::MINB) fstage_kernel(FP
     uint4 *dst = reinterpret_cast<uint4 *>(stage);
     for (int i = tid; i < nvec; i += NT) dst[i] = __ldg(&src[i]);
     const float c0 = cst[0], c1 = cst[1], cstep = cst[2], cf = cst[3];
-    for (int k = tid; k < job.substride; k += NT) {
+    for (int k = tid; k < SUB; k += NT) {
       float sn, cs;
       sincospif(-2.0f * fmaf((float)k, c1, c0), &sn, &cs);
       tsub[k] = make_float2(cs, sn);
     }
-    for (int i = tid; i < job.stride; i += NT) {
+    for (int i = tid; i < STRIDE; i += NT) {
       float sn, cs;
       sincospif(-2.0f * ((float)i * cstep), &sn, &cs);
       tstep[i] = make_float2(cs, sn);
+      sincospif(2.0f * ((float)(i * FSUB) * cf), &sn, &cs);
+      fstept[i] = make_float2(cs, sn);
     }
-    for (int k = tid; k < job.fsub; k += NT) {
+    for (int k = tid; k < FSUB; k += NT) {
       float sn, cs;
       sincospif(2.0f * ((float)k * cf), &sn, &cs);
       fsubt[k] = make_float2(cs, sn);
-    }
-    for (int i = tid; i < job.fstride; i += NT) {
-      float sn, cs;
-      sincospif(2.0f * ((float)(i << prm.fsub_shift) * cf), &sn, &cs);
-      fstept[i] = make_float2(cs, sn);
     }
   }
   __syncthreads();
 
   const bool active = tid < NTW;
-  const long long off = g.offset;
-  const int sbase = (int)(CPLX ? (4LL * off - stage_base) : ((off >> 1) - stage_base));
-
-  {
-    const int pass_pol = cpol;
-    float2 u[32];
-    // ---- first pass (P = 1): decode + rotate from the staged window
-    if (active) {
-      constexpr int NB = N / R0;
+  const int off = g.offset;
+  float2 u[32];
+  // ---- pass 0 (span 1): decode + fringe-rotate from the staged window
+  if (active) {
+    constexpr int NB = N / R0;
+    const int sbase = (int)(CPLX ? (4LL * off - stage_base) : (((long long)off >> 1) - stage_base));
 #pragma unroll
-      for (int q = 0; q < 32 / R0; q++) {
-        const int vb = tid + q * NTW;
-        const int pol = (POLS == 2) ? vb / NB : pass_pol;
-        const int iv = vb & (NB - 1);
+    for (int q = 0; q < 32 / R0; q++) {
+      const int iv = tid + q * NTW;
+      float2 *v = &u[q * R0];
+      // this thread's samples n = iv + r*NB: fine rotator index fixed, coarse index strided
+      const float2 rs = tsub[iv & (SUB - 1)];
+      const int p0 = (off & 1) + iv;  // 2-bit: sample index relative to byte off/2
+      const int shift = 2 * (2 * (p0 & 1) + pol);
 #pragma unroll
-        for (int r = 0; r < R0; r++) {
-          const int n = iv + r * NB;
-          const float2 rot = cmul(tsub[n & prm.sub_mask], tstep[n >> prm.sub_shift]);
-          float2 x;
-          if constexpr (CPLX) {
-            // int8 (A.re, A.im, B.re, B.im) per time sample
-            const char2 v = *reinterpret_cast<const char2 *>(stage + sbase + 4 * n + 2 * pol);
-            x = cmul(make_float2((float)v.x, (float)v.y), rot);
-          } else {
-            // 2-bit: byte m/2 holds A_m', B_m', A_m'+1, B_m'+1 (fxkernel.cpp:443-476)
-            const int m = (int)(off & 1) + n;  // sample index relative to byte (off >> 1)
-            const int byte = stage[sbase + (m >> 1)];
-            const int code = (byte >> (2 * (2 * (m & 1) + pol))) & 3;
-            const float v = level2bit(code);
-            x = make_float2(v * rot.x, v * rot.y);
-          }
-          u[q * R0 + r] = x;
+      for (int r = 0; r < R0; r++) {
+        const int n = iv + r * NB;
+        float2 rot;
+        if constexpr (NB % SUB == 0) rot = cmul(rs, tstep[(iv / SUB) + r * (NB / SUB)]);
+        else rot = cmul(tsub[n & (SUB - 1)], tstep[n / SUB]);
+        if constexpr (CPLX) {
+          // int8 (A.re, A.im, B.re, B.im) per time sample
+          const char2 x = *reinterpret_cast<const char2 *>(stage + sbase + 4 * iv + 2 * pol + r * (4 * NB));
+          v[r] = cmul(make_float2((float)x.x, (float)x.y), rot);
+        } else {
+          // 2-bit: byte m/2 holds A_m', B_m', A_m'+1, B_m'+1 (fxkernel.cpp:443-476)
+          const int byte = stage[sbase + (p0 >> 1) + r * (NB / 2)];
+          const float lv = level2bit((byte >> shift) & 3);
+          v[r] = make_float2(lv * rot.x, lv * rot.y);
         }
-        dft<R0>(&u[q * R0]);
+      }
+      dft<R0>(v);
+    }
+  }
+  __syncthreads();  // (the staged window and tables stay in place; nothing else to wait for)
+  // store pass 0: element j + r with j = iv*R0, padded index iv*(R0+1) + r
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < 32 / R0; q++) {
+      const int iv = tid + q * NTW;
+      float2 *b = buf + iv * (R0 + 1);
+#pragma unroll
+      for (int r = 0; r < R0; r++) b[r] = u[q * R0 + r];
+    }
+  }
+  __syncthreads();
+  // ---- middle pass (3-pass schedules): radix R1, span R0
+  if constexpr (R2 > 1) {
+    constexpr int NB = N / R1;
+    static_assert(NB % PAD == 0, "padding");
+    if (active) {
+#pragma unroll
+      for (int q = 0; q < 32 / R1; q++) {
+        const int iv = tid + q * NTW;
+        const float2 *b = buf + iv + iv / PAD;
+#pragma unroll
+        for (int r = 0; r < R1; r++) u[q * R1 + r] = b[r * (NB + NB / PAD)];
+        twiddle<N, R1, R0>(&u[q * R1], iv & (R0 - 1), prm.tw);
+        dft<R1>(&u[q * R1]);
       }
     }
-    if (active) pass_store<N, R0, 1, NTW, POLS, PAD0>(buf, u, tid);
     __syncthreads();
-    if constexpr (R2 > 1) {
-      if (active) pass_load<N, R1, R0, NTW, POLS, PAD0>(buf, prm.tw, u, tid);
-      __syncthreads();
-      if (active) pass_store<N, R1, R0, NTW, POLS, 32>(buf, u, tid);
-      __syncthreads();
-    }
-    // ---- last pass: outputs c = iv + r*N/RL go straight to global
     if (active) {
-      pass_load<N, RL, PL, NTW, POLS, (R2 > 1 ? 32 : PAD0)>(buf, prm.tw, u, tid);
-      constexpr int NB = N / RL;
 #pragma unroll
-      for (int q = 0; q < 32 / RL; q++) {
-        const int vb = tid + q * NTW;
-        const int pol = (POLS == 2) ? vb / NB : pass_pol;
-        const int iv = vb & (NB - 1);
-        const int s = 2 * ant + pol;
+      for (int q = 0; q < 32 / R1; q++) {
+        const int iv = tid + q * NTW;
+        const int k = iv & (R0 - 1);
+        const int j = (iv - k) * R1 + k;
+        float2 *b = buf + j + j / PAD;
 #pragma unroll
-        for (int r = 0; r < RL; r++) {
-          const int c = iv + r * NB;
-          if (c < nchan) {
-            const float2 fr = cmul(fsubt[c & prm.fsub_mask], fstept[c >> prm.fsub_shift]);
-            const float2 y = cmul(u[q * RL + r], fr);
-            const size_t o = (((size_t)(c >> 4) * prm.T + tl) * nstreams + s) * CW + (c & 15);
-            chan[o] = to_out<OutT>(y, prm.out_scale);
-          }
-        }
+        for (int r = 0; r < R1; r++) b[r * (R0 + R0 / PAD)] = u[q * R1 + r];
+      }
+    }
+    __syncthreads();
+  }
+  // ---- last pass: radix RL, span PL = N/RL (32/RL butterflies per thread);
+  //      outputs c = iv + r*NB go straight to global
+  if (active) {
+    constexpr int PL = N / RL, NB = N / RL;
+    static_assert(NB % PAD == 0 && NB % 16 == 0, "padding / channel tiles");
+    constexpr int RKEEP = CPLX ? RL : RL / 2;  // real data keeps channels c < N/2
+#pragma unroll
+    for (int q = 0; q < 32 / RL; q++) {
+      const int iv = tid + q * NTW;
+      float2 *v = &u[q * RL];
+      const float2 *b = buf + iv + iv / PAD;
+#pragma unroll
+      for (int r = 0; r < RL; r++) v[r] = b[r * (NB + NB / PAD)];
+      twiddle<N, RL, PL>(v, iv, prm.tw);
+      dft<RL>(v);
+      const float2 fs = fsubt[iv & (FSUB - 1)];
+      OutT *o = out0 + (size_t)(iv >> 4) * ctile_stride + (iv & 15);
+#pragma unroll
+      for (int r = 0; r < RKEEP; r++) {
+        const int c = iv + r * NB;
+        float2 fr;
+        if constexpr (NB % FSUB == 0) fr = cmul(fs, fstept[(iv / FSUB) + r * (NB / FSUB)]);
+        else fr = cmul(fsubt[c & (FSUB - 1)], fstept[c / FSUB]);
+        o[(size_t)r * (NB / 16) * ctile_stride] = to_out<OutT>(cmul(v[r], fr), prm.out_scale);
       }
     }
   }
@@ -485,11 +497,14 @@ __global__ void __launch_bounds__(FPlan<L>::NT, FPlan<L>::MINB) fstage_kernel(FP
 
 template <int L, typename OutT, bool CPLX>
 static cudaError_t launch_fstage_t(const FParams &prm, int nt, cudaStream_t s) {
-  using Pl = FPlan<L>;
+  using Pl = FPlan<L, CPLX>;
   const Job &job = prm.job;
+  if (job.substride != Pl::SUB || job.stride != Pl::STRIDE || job.fsub != Pl::FSUB || job.fstride != Pl::STRIDE ||
+      job.nchan != Pl::NCHAN)
+    return cudaErrorInvalidValue;
   const size_t stage_bytes = CPLX ? 4 * (size_t)Pl::N + 32 : (size_t)Pl::N / 2 + 32;
-  const size_t smem = sizeof(float2) * ((size_t)Pl::POLS * Pl::PADN + job.substride + job.stride + job.fsub +
-                                        job.fstride) + ((stage_bytes + 15) & ~(size_t)15);
+  const size_t smem = sizeof(float2) * ((size_t)Pl::PADN + Pl::SUB + 2 * Pl::STRIDE + Pl::FSUB) +
+                      ((stage_bytes + 15) & ~(size_t)15);
   auto kern = fstage_kernel<L, OutT, CPLX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

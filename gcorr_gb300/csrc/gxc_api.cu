@@ -328,8 +328,9 @@ gxc_status gxc_set_input(gxc_handle *h, const uint8_t *const *per_ant, size_t by
       continue;
     }
     if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) {
-      if (h->cfg.is_complex && ((uintptr_t)per_ant[a] & 1u))
-        return fail(h, GXC_ERR_INVALID_ARGUMENT, "8-bit complex device input must be 2-byte aligned");
+      // the F-stage stages each FFT window with 16-byte vector loads
+      if ((uintptr_t)per_ant[a] & 15u)
+        return fail(h, GXC_ERR_INVALID_ARGUMENT, "device input buffers must be 16-byte aligned");
       n_dev++;
     } else {
       n_host++;

@@ -137,3 +137,14 @@ def test_call_order_errors():
     with pytest.raises(GxcError):
         fx.process()
     fx.close()
+
+
+def test_misaligned_device_input_is_rejected_before_any_launch():
+    import torch
+    from gcorr_gb300 import GxcError
+    w = synth.Workload(nant=2, nchan=256, nfft=4, bw_hz=32e6, seed=3)
+    fx = FxKernel(w.nant, w.nchan, w.nfft, 2, w.lo_hz, w.bw_hz, False)
+    big = torch.zeros(w.bytes_per_antenna + 64, dtype=torch.uint8, device="cuda")
+    with pytest.raises(GxcError):
+        fx.setInputData([big[1:1 + w.bytes_per_antenna], big[1:1 + w.bytes_per_antenna]])
+    fx.close()
