@@ -225,6 +225,7 @@ def main():
     ap.add_argument("--nfft", type=int, default=0, help="override the FFT count (small profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-xcompare", action="store_true")
     ap.add_argument("--ref-step-s", type=float, default=6.0)
     ap.add_argument("--out-dir", default=os.path.join(ROOT, "gpurun_out"))
     args = ap.parse_args()
@@ -290,6 +291,35 @@ def main():
     f_ms, x_ms, tot_ms = fx.stage_times()
     fx.enable_stage_timing(False)
     vis0 = fx.visibilities()
+
+    # X-stage comparison (untimed): the same sub-integration through each X engine
+    xcmp = {}
+    if not args.no_xcompare:
+        for name, prec, eng in (("fp32_cuda_core", "fp32", "cuda_core"), ("fp32_tensor_split", "fp32", "tensor"),
+                                ("fp16_tensor", "fp16", "tensor")):
+            try:
+                fy = G.FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=prec,
+                                rotator="exact", autos=True, x_engine=eng, fft_block=args.fft_block, device=local)
+            except Exception as ex:  # engine not available for this shape
+                xcmp[name] = {"error": str(ex)[:120]}
+                continue
+            fy.setInputData(inputs_dev)
+            fy.setDelays(d["poly"], d["fso"])
+            fy.enable_stage_timing(True)
+            fy.process(stream=sptr, sync=False)
+            fy.sync()
+            fy.process(stream=sptr, sync=False)
+            a, b, c = fy.stage_times()
+            v = fy.visibilities()
+            den = float(np.sqrt(np.sum(np.abs(vis0.astype(np.complex128)) ** 2)))
+            xcmp[name] = {"x_ms": b, "f_ms": a, "total_ms": c,
+                          "rel_rms_vs_default": float(np.sqrt(np.sum(np.abs(v - vis0) ** 2)) / max(den, 1e-30))}
+            fy.close()
+        if "fp32_cuda_core" in xcmp and "x_ms" in xcmp["fp32_cuda_core"]:
+            base = xcmp["fp32_cuda_core"]["x_ms"]
+            for k_, v_ in xcmp.items():
+                if "x_ms" in v_:
+                    v_["speedup_vs_fp32_cuda_core"] = base / v_["x_ms"]
 
     samples = w.nant * 2 * w.nfft * w.fft_len
     value = samples * world / (ms_max / 1e3) / 1e9
@@ -371,6 +401,7 @@ def main():
                        "l2": f"inputs larger than L2 ({in_bytes / 1e9:.1f} GB packed, "
                              f"{chan_bytes / 1e9:.1f} GB channelised per step)"},
             "stage_ms": {"f": f_ms, "x": x_ms, "total": tot_ms},
+            "x_engines": xcmp,
             "x_tflops": xflops / (x_ms / 1e3) / 1e12,
             "gpu_launches": launches_per_step * args.steps,
             "roofline": roof,

@@ -113,8 +113,10 @@ std::string validate(const gxc_config *c, gxc_status *st) {
   if (!fstage_supported((int)F)) return "FFT length outside 256..16384";
   if (c->precision == GXC_PRECISION_FP8) return "FP8 channelised data is not implemented";
   if (c->x_engine == GXC_XENGINE_TENSOR) {
-    if (c->precision != GXC_PRECISION_FP16) return "the tensor-core X-stage takes FP16 channelised data";
-    if (!xstage_tensor_supported(c->nant)) return "tensor-core X-stage: nant outside the supported range";
+    if (!xstage_tensor_supported(c->nant)) return "tensor-core X-stage: needs 4*nant <= 128";
+    const int ct = c->precision == GXC_PRECISION_FP32 ? CHAN_F32 : CHAN_F16;
+    if (c->nchan % xstage_tensor_channels_per_cta(c->nant, ct))
+      return "tensor-core X-stage: nchan must be a multiple of its channel tile";
   }
   *st = GXC_OK;
   return "";
@@ -220,9 +222,14 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   h->bytes_per_ant = input_bytes(cfg);
   h->chan_type = (cfg->precision == GXC_PRECISION_FP32) ? CHAN_F32 : CHAN_F16;
   h->xeng = cfg->x_engine;
+  // AUTO: tensor cores for FP16 data; FP32 data stays on CUDA cores (FP32 FMAs,
+  // round-to-nearest), because tensor-core accumulation in TMEM rounds towards
+  // zero and its bias grows with the number of accumulated FFTs.
   if (h->xeng == GXC_XENGINE_AUTO)
-    h->xeng = (cfg->precision == GXC_PRECISION_FP16 && xstage_tensor_supported(nant)) ? GXC_XENGINE_TENSOR
-                                                                                       : GXC_XENGINE_CUDA_CORE;
+    h->xeng = (h->chan_type == CHAN_F16 && xstage_tensor_supported(nant) &&
+               cfg->nchan % xstage_tensor_channels_per_cta(nant, h->chan_type) == 0)
+                  ? GXC_XENGINE_TENSOR
+                  : GXC_XENGINE_CUDA_CORE;
   // FP16 storage keeps |X| near the sample rms: scale by 2^-floor(log2(F)/2),
   // an exact power of two undone exactly at finalisation.
   if (h->chan_type == CHAN_F16) {
@@ -438,7 +445,9 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
     if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b + 1], s), "timing event");
     if (h->nbl > 0) {
       if (h->xeng == GXC_XENGINE_TENSOR) {
-        GXC_CUDA(h, launch_xstage_tensor(h->d_chan, nant, c.nchan, h->T, nt, c.autos, h->d_vsum, h->d_vcomp, s),
+        GXC_CUDA(h,
+                 launch_xstage_tensor(h->d_chan, h->chan_type, nant, c.nchan, h->T, nt, c.autos, h->d_vsum,
+                                      h->d_vcomp, s),
                  "tensor-core X-stage kernel");
       } else {
         GXC_CUDA(h,

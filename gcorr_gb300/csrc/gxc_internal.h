@@ -61,9 +61,11 @@ cudaError_t launch_xstage_cuda_core_pairs(const void *chan, int chan_type, int n
                                           cudaStream_t s);
 
 // xstage_tc.cu: tcgen05 tensor-core X-stage over FP16 channelised data.
-cudaError_t launch_xstage_tensor(const void *chan, int nant, int nchan, int T, int nt, int autos, float2 *vsum,
-                                 float2 *vcomp, cudaStream_t s);
+// FP16 data: kind::f16 MMAs; FP32 data: kind::tf32 MMAs on a hi/lo split (FP32-accurate products).
+cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,
+                                 float2 *vsum, float2 *vcomp, cudaStream_t s);
 int xstage_tensor_supported(int nant);
+int xstage_tensor_channels_per_cta(int nant, int chan_type);
 cudaError_t xstage_tensor_take_error(int *flag);
 
 // Output baseline index of antennas j <= k (crosses in fxkernel order, then autos).

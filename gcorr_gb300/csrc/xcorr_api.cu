@@ -80,7 +80,7 @@ gxc_status xcorr_run(const float2 *ants, int nant, int nfft, int nchan, int fftw
     e = cudaGetLastError();
     if (e != cudaSuccess) break;
     if (engine == GXC_XENGINE_TENSOR)
-      e = launch_xstage_tensor(chan, nant, nchan, T, nt, autos, vsum, vcomp, s);
+      e = launch_xstage_tensor(chan, ct, nant, nchan, T, nt, autos, vsum, vcomp, s);
     else
       e = launch_xstage_cuda_core(chan, ct, nant, nchan, T, nt, autos, vsum, vcomp, s);
   }
@@ -104,20 +104,12 @@ gxc_status xcorr_check(int nant, int nfft, int nchan, int fftwidth, int precisio
     *msg = "gxc_xcorr: precision must be FP32 or FP16";
     return GXC_ERR_UNSUPPORTED;
   }
-  if (*engine == GXC_XENGINE_AUTO)
-    *engine = (precision == GXC_PRECISION_FP16 && xstage_tensor_supported(nant)) ? GXC_XENGINE_TENSOR
-                                                                                  : GXC_XENGINE_CUDA_CORE;
-  if (*engine == GXC_XENGINE_TENSOR) {
-    if (precision != GXC_PRECISION_FP16 || !xstage_tensor_supported(nant)) {
-      *msg = "gxc_xcorr: the tensor-core X-stage takes FP16 and 4*nant <= 128";
-      return GXC_ERR_UNSUPPORTED;
-    }
-    int R = 16;
-    while (R < 4 * nant) R <<= 1;
-    if (nchan % (4 * (128 / R))) {
-      *msg = "gxc_xcorr: nchan must be a multiple of the tensor-core channel tile";
-      return GXC_ERR_UNSUPPORTED;
-    }
+  const int ct = precision == GXC_PRECISION_FP32 ? CHAN_F32 : CHAN_F16;
+  const bool tc_ok = xstage_tensor_supported(nant) && nchan % xstage_tensor_channels_per_cta(nant, ct) == 0;
+  if (*engine == GXC_XENGINE_AUTO) *engine = tc_ok ? GXC_XENGINE_TENSOR : GXC_XENGINE_CUDA_CORE;
+  if (*engine == GXC_XENGINE_TENSOR && !tc_ok) {
+    *msg = "gxc_xcorr: the tensor-core X-stage needs 4*nant <= 128 and nchan a multiple of its channel tile";
+    return GXC_ERR_UNSUPPORTED;
   }
   return GXC_OK;
 }

@@ -28,16 +28,28 @@ namespace gxc {
 
 namespace tc {
 
-constexpr int KC = 64;            // FFTs (K) per smem stage: one 128-byte swizzle row of FP16
-constexpr int NG = 4;             // MMA groups (128 TMEM columns each)
 constexpr int STAGES = 3;
-constexpr int GROUP_BYTES = 128 * 128;           // 128 rows x 128 bytes
-constexpr int STAGE_BYTES = NG * GROUP_BYTES;    // 64 KiB
+constexpr int TILE_BYTES = 128 * 128;            // 128 rows x 128 bytes (one SW128 K-major tile)
 constexpr int NPROD_WARPS = 8;
 constexpr int NPROD = NPROD_WARPS * 32;
 constexpr int NTHREADS = NPROD + 32;
-constexpr int TMEM_COLS = 512;
 constexpr unsigned long long WAIT_NS = 4000000000ull;  // 4 s
+
+// FP16 path: one FP16 tile per group, K = 64 FFTs per stage, 4 groups (512 TMEM columns).
+// SPLIT path (FP32 data): each value x is split into hi = TF32(x) (low 13 mantissa
+// bits cleared) and lo = x - hi (exact); hi.hi^T + lo.hi^T + hi.lo^T is accumulated
+// in FP32 with kind::tf32 MMAs (every product exact, relative error ~2^-20).
+// Two tiles (hi, lo) per group, K = 32 FFTs per stage, 2 groups (256 TMEM columns).
+template <bool SPLIT>
+struct Cfg {
+  static constexpr int KC = SPLIT ? 32 : 64;
+  static constexpr int NG = SPLIT ? 2 : 4;
+  static constexpr int TILES = SPLIT ? 2 : 1;
+  static constexpr int KSTEP = SPLIT ? 8 : 16;
+  static constexpr int GROUP_BYTES = TILES * TILE_BYTES;
+  static constexpr int STAGE_BYTES = NG * GROUP_BYTES;  // 64 KiB
+  static constexpr int TMEM_COLS = NG * 128;
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -120,6 +132,17 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_
       : "memory");
 }
 
+// D[tmem] (+)= A[smem] * B[smem]^T, kind::tf32 (FP32 operands read as TF32, FP32 accumulate).
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 // Arrives on the mbarrier once every previously issued tcgen05.mma of this thread completed.
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
@@ -152,8 +175,10 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor, kind::f16: D = F32, A = B = F16, both K-major, M = N = 128.
+// Instruction descriptors: D = F32, both operands K-major, M = N = 128;
+// A = B = F16 (kind::f16) or A = B = TF32 (kind::tf32, format code 2).
 constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t IDESC_TF32 = (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
 
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
   uint32_t r;
@@ -162,14 +187,18 @@ __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
 }
 
 struct Params {
-  const __half2 *chan;  // [ctile][T][n][16]
+  const void *chan;     // [ctile][T][n][16] half2 (FP16 path) or float2 (SPLIT path)
   int nant, nstream, nchan, T, nt, autos;
   int R, g, CS;         // rows per channel block, channels per MMA group, channels per CTA
   float2 *vsum, *vcomp;
   int *err;
 };
 
+template <bool SPLIT>
 __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
+  using C = Cfg<SPLIT>;
+  constexpr int KC = C::KC, NG = C::NG, GROUP_BYTES = C::GROUP_BYTES, STAGE_BYTES = C::STAGE_BYTES;
+  constexpr int TMEM_COLS = C::TMEM_COLS;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_done;
   __shared__ uint32_t tmem_base_sh;
@@ -205,8 +234,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
 
   if (warp < NPROD_WARPS) {
     // ------------------------------------------------------------ producers
-    const int nq = p.CS / 4;                  // channel quads of this CTA
-    const int ntask = 8 * n * nq;             // (octet, stream, quad) per chunk
+    // FP16: channel quads (CS >= 4); SPLIT: channel pairs (CS >= 2)
+    const int nq = SPLIT ? p.CS / 2 : p.CS / 4;
+    const int ntask = 8 * n * nq;             // (16-byte chunk, stream, channel group) per stage
     for (int ch = 0; ch < nchunks; ch++) {
       const int st = ch % STAGES;
       if (ch >= STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err)) break;
@@ -216,32 +246,67 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
         const int q = task % nq;
         const int rest = task / nq;
         const int s = rest % n;
-        const int o = rest / n;
-        const int c = cb + 4 * q;
-        const int ctile = c >> 4, coff = c & 15;
-        const __half2 *src = p.chan + ((size_t)ctile * p.T * n + s) * CW + coff;
-        uint4 v[8];
+        const int o = rest / n;  // 16-byte chunk of the 128-byte K row
+        if constexpr (!SPLIT) {
+          const int c = cb + 4 * q;
+          const int ctile = c >> 4, coff = c & 15;
+          // 8 FFTs x 4 channels of FP16 complex -> 8 rows (4 channels x re/im) of 8 FFTs
+          const __half2 *src = (const __half2 *)p.chan + ((size_t)ctile * p.T * n + s) * CW + coff;
+          uint4 v[8];
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-          const int t = tb + 8 * o + i;
-          v[i] = (t < p.nt) ? __ldg(reinterpret_cast<const uint4 *>(src + (size_t)t * n * CW))
-                            : make_uint4(0, 0, 0, 0);
-        }
+          for (int i = 0; i < 8; i++) {
+            const int t = tb + 8 * o + i;
+            v[i] = (t < p.nt) ? __ldg(reinterpret_cast<const uint4 *>(src + (size_t)t * n * CW))
+                              : make_uint4(0, 0, 0, 0);
+          }
 #pragma unroll
-        for (int ci = 0; ci < 4; ci++) {
-          const int cc = 4 * q + ci;
-          const int G = cc / p.g, gi = cc - G * p.g;
-          const int row = gi * p.R + 2 * s;
-          uint32_t w[8];
+          for (int ci = 0; ci < 4; ci++) {
+            const int cc = 4 * q + ci;
+            const int G = cc / p.g, gi = cc - G * p.g;
+            const int row = gi * p.R + 2 * s;
+            uint32_t w[8];
 #pragma unroll
-          for (int i = 0; i < 8; i++) w[i] = (ci == 0) ? v[i].x : (ci == 1) ? v[i].y : (ci == 2) ? v[i].z : v[i].w;
-          const uint4 re = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410), prmt(w[4], w[5], 0x5410),
-                                      prmt(w[6], w[7], 0x5410));
-          const uint4 im = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632), prmt(w[4], w[5], 0x7632),
-                                      prmt(w[6], w[7], 0x7632));
-          unsigned char *gbase = stage + G * GROUP_BYTES;
-          *reinterpret_cast<uint4 *>(gbase + row * 128 + ((o ^ (row & 7)) << 4)) = re;
-          *reinterpret_cast<uint4 *>(gbase + (row + 1) * 128 + ((o ^ ((row + 1) & 7)) << 4)) = im;
+            for (int i = 0; i < 8; i++) w[i] = (ci == 0) ? v[i].x : (ci == 1) ? v[i].y : (ci == 2) ? v[i].z : v[i].w;
+            const uint4 re = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410),
+                                        prmt(w[4], w[5], 0x5410), prmt(w[6], w[7], 0x5410));
+            const uint4 im = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632),
+                                        prmt(w[4], w[5], 0x7632), prmt(w[6], w[7], 0x7632));
+            unsigned char *gbase = stage + G * GROUP_BYTES;
+            *reinterpret_cast<uint4 *>(gbase + row * 128 + ((o ^ (row & 7)) << 4)) = re;
+            *reinterpret_cast<uint4 *>(gbase + (row + 1) * 128 + ((o ^ ((row + 1) & 7)) << 4)) = im;
+          }
+        } else {
+          // 4 FFTs x 2 channels of FP32 complex -> 4 rows of 4 FFTs, each split into hi and lo tiles
+          const int c2 = cb + 2 * q;
+          const int ctile2 = c2 >> 4, coff2 = c2 & 15;
+          const float2 *src = (const float2 *)p.chan + ((size_t)ctile2 * p.T * n + s) * CW + coff2;
+          float4 v[4];
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            const int t = tb + 4 * o + i;
+            v[i] = (t < p.nt) ? __ldg(reinterpret_cast<const float4 *>(src + (size_t)t * n * CW))
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+#pragma unroll
+          for (int ci = 0; ci < 2; ci++) {
+            const int cc = 2 * q + ci;
+            const int G = cc / p.g, gi = cc - G * p.g;
+#pragma unroll
+            for (int part = 0; part < 2; part++) {
+              const int row = gi * p.R + 2 * s + part;
+              uint32_t hi[4], lo[4];
+#pragma unroll
+              for (int i = 0; i < 4; i++) {
+                const float x = ci ? (part ? v[i].w : v[i].z) : (part ? v[i].y : v[i].x);
+                hi[i] = __float_as_uint(x) & 0xFFFFE000u;
+                lo[i] = __float_as_uint(x - __uint_as_float(hi[i]));
+              }
+              unsigned char *gbase = stage + G * GROUP_BYTES;
+              const int sw = (o ^ (row & 7)) << 4;
+              *reinterpret_cast<uint4 *>(gbase + row * 128 + sw) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+              *reinterpret_cast<uint4 *>(gbase + TILE_BYTES + row * 128 + sw) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+            }
+          }
         }
       }
       fence_proxy_async_smem();
@@ -257,9 +322,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
 #pragma unroll
       for (int G = 0; G < NG; G++) {
 #pragma unroll
-        for (int kk = 0; kk < KC / 16; kk++) {
-          const uint64_t d = desc_sw128(sa + G * GROUP_BYTES + kk * 32);
-          mma_f16(tmem + G * 128, d, d, IDESC, (ch > 0 || kk > 0) ? 1u : 0u);
+        for (int kk = 0; kk < KC / C::KSTEP; kk++) {
+          const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
+          const uint64_t dh = desc_sw128(sa + G * GROUP_BYTES + kk * 32);
+          if constexpr (!SPLIT) {
+            mma_f16(tmem + G * 128, dh, dh, IDESC, acc);
+          } else {
+            const uint64_t dl = desc_sw128(sa + G * GROUP_BYTES + TILE_BYTES + kk * 32);
+            mma_tf32(tmem + G * 128, dh, dh, IDESC_TF32, acc);
+            mma_tf32(tmem + G * 128, dl, dh, IDESC_TF32, 1u);
+            mma_tf32(tmem + G * 128, dh, dl, IDESC_TF32, 1u);
+          }
         }
       }
       mma_commit(smem_u32(&bar_empty[st]));
@@ -359,12 +432,19 @@ cudaError_t xstage_tensor_take_error(int *flag) {
   return e;
 }
 
-cudaError_t launch_xstage_tensor(const void *chan, int nant, int nchan, int T, int nt, int autos, float2 *vsum,
-                                 float2 *vcomp, cudaStream_t s) {
+// Channels per CTA of the tensor-core X-stage for nant antennas (the channel count must divide by it).
+int xstage_tensor_channels_per_cta(int nant, int chan_type) {
+  int R = 16;
+  while (R < 4 * nant) R <<= 1;  // 2 rows (re, im) per stream, 2 streams per antenna
+  return (chan_type == CHAN_F32 ? tc::Cfg<true>::NG : tc::Cfg<false>::NG) * (128 / R);
+}
+
+cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,
+                                 float2 *vsum, float2 *vcomp, cudaStream_t s) {
   if (nt <= 0) return cudaSuccess;
   if (!xstage_tensor_supported(nant)) return cudaErrorInvalidValue;
   tc::Params p;
-  p.chan = (const __half2 *)chan;
+  p.chan = chan;
   p.nant = nant;
   p.nstream = 2 * nant;
   p.nchan = nchan;
@@ -375,16 +455,23 @@ cudaError_t launch_xstage_tensor(const void *chan, int nant, int nchan, int T, i
   while (R < 2 * p.nstream) R <<= 1;  // 2 rows (re, im) per stream
   p.R = R;
   p.g = 128 / R;
-  p.CS = 4 * p.g;
+  p.CS = xstage_tensor_channels_per_cta(nant, chan_type);
   if (nchan % p.CS) return cudaErrorInvalidValue;
   p.vsum = vsum;
   p.vcomp = vcomp;
   cudaError_t e = xstage_tensor_error_flag(&p.err);
   if (e != cudaSuccess) return e;
-  const size_t smem = (size_t)tc::STAGES * tc::STAGE_BYTES + 1024;
-  e = cudaFuncSetAttribute(tc::xstage_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  tc::xstage_tc_kernel<<<nchan / p.CS, tc::NTHREADS, smem, s>>>(p);
+  const size_t smem = (size_t)tc::STAGES * 65536 + 1024;
+  static_assert(tc::Cfg<true>::STAGE_BYTES == 65536 && tc::Cfg<false>::STAGE_BYTES == 65536, "stage size");
+  if (chan_type == CHAN_F32) {
+    e = cudaFuncSetAttribute(tc::xstage_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    tc::xstage_tc_kernel<true><<<nchan / p.CS, tc::NTHREADS, smem, s>>>(p);
+  } else {
+    e = cudaFuncSetAttribute(tc::xstage_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    tc::xstage_tc_kernel<false><<<nchan / p.CS, tc::NTHREADS, smem, s>>>(p);
+  }
   return cudaGetLastError();
 }
 

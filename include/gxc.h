@@ -48,7 +48,11 @@ enum { GXC_PRECISION_FP32 = 0, GXC_PRECISION_FP16 = 1, GXC_PRECISION_FP8 = 2 };
 /* EXACT: linear fringe phase per sample; FXKERNEL: the reference's sub/step
  * rotator table including its real-data half-rate step (fxkernel.cpp:112,553-558). */
 enum { GXC_ROTATOR_EXACT = 0, GXC_ROTATOR_FXKERNEL = 1 };
-/* X-stage engine: AUTO picks tensor cores for FP16/FP8 and CUDA cores for FP32. */
+/* X-stage engine.  TENSOR: tcgen05 MMAs with FP32 accumulation in tensor memory;
+ * FP16 data uses kind::f16, FP32 data a hi/lo TF32 split (hi.hi + lo.hi + hi.lo,
+ * every product exact, ~2^-20 relative error).  CUDA_CORE: plain FP32 FMAs.
+ * AUTO: TENSOR for FP16 data when 4*nant <= 128 and nchan fits its channel tile,
+ * CUDA_CORE otherwise (FP32 data stays on round-to-nearest FP32 FMAs). */
 enum { GXC_XENGINE_AUTO = 0, GXC_XENGINE_CUDA_CORE = 1, GXC_XENGINE_TENSOR = 2 };
 enum { GXC_LAYOUT_FXKERNEL = 0 };
 
@@ -133,7 +137,7 @@ gxc_status gxc_stage_times(gxc_handle *h, float *f_ms, float *x_ms, float *total
  * (crosses in fxkernel order, then autos when autos != 0), each product
  * summed over the nfft spectra and divided by nfft as CCAH3 does
  * (gcorr/src/gxkernel.cu:574-581).  precision: GXC_PRECISION_FP32 or _FP16
- * (values cast to FP16 unscaled); x_engine: GXC_XENGINE_*.  Synchronous on
+ * (values cast to FP16 unscaled); x_engine: GXC_XENGINE_* (as for gxc_config).  Synchronous on
  * `stream`; allocates its scratch with cudaMalloc. */
 gxc_status gxc_xcorr(const float *ants, int nant, int nfft, int nchan, int fftwidth, int precision, int x_engine,
                      int autos, float *accum, void *stream);

@@ -34,10 +34,12 @@ def _wd(w: synth.Workload):
                 bw_hz=w.bw_hz)
 
 
-def test_golden_fxkernel_mode_matches_reference(golden_cases):
+@pytest.mark.parametrize("engine", ["tensor", "cuda_core"])
+def test_golden_fxkernel_mode_matches_reference(golden_cases, engine):
     """fxkernel rotator, crosses only: the reference's own process() output."""
     for name, d in golden_cases.items():
-        vis, counts, flags = _run(d, d["inputs"], d["poly"], d["fso"], rotator="fxkernel", autos=False)
+        vis, counts, flags = _run(d, d["inputs"], d["poly"], d["fso"], rotator="fxkernel", autos=False,
+                                  x_engine=engine)
         ref = d["ref_vis"]
         assert vis.shape == ref.shape
         err = O.rel_rms_per_product(vis, ref)
@@ -47,9 +49,10 @@ def test_golden_fxkernel_mode_matches_reference(golden_cases):
         assert np.array_equal(flags, d["geom"][..., 1].astype(np.uint8)), name
 
 
-def test_golden_exact_mode_matches_fp64_oracle(golden_cases):
+@pytest.mark.parametrize("engine", ["tensor", "cuda_core"])
+def test_golden_exact_mode_matches_fp64_oracle(golden_cases, engine):
     for name, d in golden_cases.items():
-        vis, counts, _ = _run(d, d["inputs"], d["poly"], d["fso"], rotator="exact", autos=True)
+        vis, counts, _ = _run(d, d["inputs"], d["poly"], d["fso"], rotator="exact", autos=True, x_engine=engine)
         err = O.rel_rms_per_product(vis, d["exact_vis"])
         assert err.max() < FP32_TOL, (name, err.max())
         assert np.array_equal(counts, d["exact_counts"]), name
@@ -148,3 +151,18 @@ def test_misaligned_device_input_is_rejected_before_any_launch():
     with pytest.raises(GxcError):
         fx.setInputData([big[1:1 + w.bytes_per_antenna], big[1:1 + w.bytes_per_antenna]])
     fx.close()
+
+
+@pytest.mark.parametrize("precision,engine,tol", [("fp32", "cuda_core", FP32_TOL), ("fp16", "tensor", FP16_TOL),
+                                                  ("fp16", "cuda_core", FP16_TOL)])
+def test_long_integration_accuracy_vs_fp64(precision, engine, tol):
+    """8192 FFTs accumulated in one block: the accumulation error must stay inside
+    the tolerance of the precision (per baseline and product, autos included)."""
+    w = synth.Workload(nant=4, nchan=256, nfft=8192, bw_hz=32e6, rho=0.05, seed=5)
+    d = synth.generate(w)
+    inputs = [x.numpy() for x in d["inputs"]]
+    ref, rc = O.exact_process(O.config_from_workload(w, O.ROT_EXACT, True), inputs, d["poly"], d["fso"])
+    vis, counts, _ = _run(_wd(w), inputs, d["poly"], d["fso"], precision=precision, x_engine=engine,
+                          fft_block=w.nfft)
+    assert np.array_equal(counts, rc)
+    assert O.rel_rms_per_product(vis, ref).max() < tol

@@ -51,6 +51,7 @@ def xcorr(data, nant, nfft, nchan, fftwidth, precision, engine, autos=False):
 
 
 ENGINES = [("fp32-cuda-core", L.GXC_PRECISION_FP32, L.GXC_XENGINE_CUDA_CORE),
+           ("fp32-tensor-split", L.GXC_PRECISION_FP32, L.GXC_XENGINE_TENSOR),
            ("fp16-cuda-core", L.GXC_PRECISION_FP16, L.GXC_XENGINE_CUDA_CORE),
            ("fp16-tensor", L.GXC_PRECISION_FP16, L.GXC_XENGINE_TENSOR)]
 
@@ -106,3 +107,17 @@ def test_tensor_is_default_for_fp16():
     v = fx.visibilities()
     assert np.isfinite(v).all()
     fx.close()
+
+
+@pytest.mark.parametrize("nant", [1, 3, 8, 16, 32])
+def test_tensor_split_fp32_matches_cuda_core_fp32(nant):
+    """FP32 data: the TF32 hi/lo split on tensor cores agrees with FP32 FMAs to FP32 accuracy."""
+    nchan, fftwidth, nfft = 128, 256, 200
+    rng = np.random.default_rng(100 + nant)
+    n = 2 * nant * fftwidth * nfft
+    data = (rng.normal(size=n) + 1j * rng.normal(size=n)).astype(np.complex64) * np.float32(37.0)
+    a = xcorr(data, nant, nfft, nchan, fftwidth, L.GXC_PRECISION_FP32, L.GXC_XENGINE_TENSOR, autos=True)
+    b = xcorr(data, nant, nfft, nchan, fftwidth, L.GXC_PRECISION_FP32, L.GXC_XENGINE_CUDA_CORE, autos=True)
+    ref = expected_crosscorraccum(data, nant, nfft, nchan, fftwidth, autos=True)
+    assert O.rel_rms_per_product(a, ref).max() < 1e-5
+    assert O.rel_rms_per_product(b, ref).max() < 1e-5
