@@ -222,12 +222,12 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   h->bytes_per_ant = input_bytes(cfg);
   h->chan_type = (cfg->precision == GXC_PRECISION_FP32) ? CHAN_F32 : CHAN_F16;
   h->xeng = cfg->x_engine;
-  // AUTO: tensor cores for FP16 data; FP32 data stays on CUDA cores (FP32 FMAs,
-  // round-to-nearest), because tensor-core accumulation in TMEM rounds towards
-  // zero and its bias grows with the number of accumulated FFTs.
+  // AUTO: tensor cores whenever the antenna count and channel tile fit.  FP32 data
+  // uses the TF32 hi/lo split, whose TMEM accumulators are drained every 128
+  // FFTs (TMEM accumulation rounds towards zero; the drains bound that bias at
+  // about 3e-6 relative, inside the FP32 tolerance, whatever the integration length).
   if (h->xeng == GXC_XENGINE_AUTO)
-    h->xeng = (h->chan_type == CHAN_F16 && xstage_tensor_supported(nant) &&
-               cfg->nchan % xstage_tensor_channels_per_cta(nant, h->chan_type) == 0)
+    h->xeng = (xstage_tensor_supported(nant) && cfg->nchan % xstage_tensor_channels_per_cta(nant, h->chan_type) == 0)
                   ? GXC_XENGINE_TENSOR
                   : GXC_XENGINE_CUDA_CORE;
   // FP16 storage keeps |X| near the sample rms: scale by 2^-floor(log2(F)/2),

@@ -398,6 +398,230 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
   if (warp == NPROD_WARPS) tmem_dealloc(tmem, TMEM_COLS);
 }
 
+
+// SPLIT path with periodic drains.  TMEM accumulation rounds towards zero, so
+// its relative bias grows with the number of MMAs accumulated; here the MMA
+// issuer alternates between two accumulator sets every DP stages (DP*KC = 128
+// FFTs) and four dedicated epilogue warps fold each finished set into
+// per-thread FP32 register sums (round-to-nearest) while the other set fills.
+// R (rows per channel block) is a template parameter so the register sums are
+// indexed at compile time.
+constexpr int NEPI_WARPS = 4;
+constexpr int NTHREADS_SPLIT = NPROD + 32 + NEPI_WARPS * 32;
+
+template <int R>
+__global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Params p) {
+  using C = Cfg<true>;
+  constexpr int KC = C::KC, NG = C::NG, GROUP_BYTES = C::GROUP_BYTES, STAGE_BYTES = C::STAGE_BYTES;
+  constexpr int NSET = 2, SET_COLS = NG * 128, TMEM_COLS = NSET * SET_COLS;  // 512
+  constexpr int DP = 4;                  // stages per drain period
+  constexpr int GCH = 128 / R;           // channels per MMA group
+  constexpr int WP = (R > 32 ? R : 32) / 16;  // 16-column pieces a warp reads per group
+  constexpr int PP = R / 16;             // pieces in one channel block
+  static_assert(TMEM_COLS == 512, "TMEM budget");
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_ready[NSET], bar_drained[NSET], bar_done;
+  __shared__ uint32_t tmem_base_sh;
+  unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t sbase = smem_u32(smem);
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int cb = blockIdx.x * p.CS;
+  const int n = p.nstream;
+  const int nchunks = (p.nt + KC - 1) / KC;
+  const int nper = (nchunks + DP - 1) / DP;
+
+  for (int i = tid; i < STAGES * STAGE_BYTES / 16; i += NTHREADS_SPLIT)
+    reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(smem_u32(&bar_full[s]), NPROD);
+      mbar_init(smem_u32(&bar_empty[s]), 1);
+    }
+    for (int b = 0; b < NSET; b++) {
+      mbar_init(smem_u32(&bar_ready[b]), 1);
+      mbar_init(smem_u32(&bar_drained[b]), NEPI_WARPS * 32);
+    }
+    mbar_init(smem_u32(&bar_done), 1);
+    fence_mbar_init();
+  }
+  if (warp == NPROD_WARPS) {
+    tmem_alloc(smem_u32(&tmem_base_sh), TMEM_COLS);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+
+  if (warp < NPROD_WARPS) {
+    // ------------------------------------------------------------ producers
+    const int nq = p.CS / 2;        // channel pairs
+    const int ntask = 8 * n * nq;   // (16-byte chunk of 4 FFTs, stream, pair) per stage
+    for (int ch = 0; ch < nchunks; ch++) {
+      const int st = ch % STAGES;
+      if (ch >= STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err)) break;
+      unsigned char *stage = smem + (size_t)st * STAGE_BYTES;
+      const int tb = ch * KC;
+      for (int task = tid; task < ntask; task += NPROD) {
+        const int q = task % nq;
+        const int rest = task / nq;
+        const int s = rest % n;
+        const int o = rest / n;
+        const int c2 = cb + 2 * q;
+        const float2 *src = (const float2 *)p.chan + ((size_t)(c2 >> 4) * p.T * n + s) * CW + (c2 & 15);
+        float4 v[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const int t = tb + 4 * o + i;
+          v[i] = (t < p.nt) ? __ldg(reinterpret_cast<const float4 *>(src + (size_t)t * n * CW))
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int ci = 0; ci < 2; ci++) {
+          const int cc = 2 * q + ci;
+          const int G = cc / GCH, gi = cc - G * GCH;
+#pragma unroll
+          for (int part = 0; part < 2; part++) {
+            const int row = gi * R + 2 * s + part;
+            uint32_t hi[4], lo[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+              const float x = ci ? (part ? v[i].w : v[i].z) : (part ? v[i].y : v[i].x);
+              hi[i] = __float_as_uint(x) & 0xFFFFE000u;
+              lo[i] = __float_as_uint(x - __uint_as_float(hi[i]));
+            }
+            unsigned char *gbase = stage + G * GROUP_BYTES;
+            const int sw = (o ^ (row & 7)) << 4;
+            *reinterpret_cast<uint4 *>(gbase + row * 128 + sw) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+            *reinterpret_cast<uint4 *>(gbase + TILE_BYTES + row * 128 + sw) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+          }
+        }
+      }
+      fence_proxy_async_smem();
+      mbar_arrive(smem_u32(&bar_full[st]));
+    }
+  } else if (warp == NPROD_WARPS) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      bool ok = true;
+      for (int ch = 0; ch < nchunks && ok; ch++) {
+        const int st = ch % STAGES;
+        const int pd = ch / DP, b = pd & 1;
+        const bool first = (ch % DP) == 0;
+        if (first && pd >= 2 && !mbar_wait(smem_u32(&bar_drained[b]), ((pd >> 1) - 1) & 1, p.err)) break;
+        if (!mbar_wait(smem_u32(&bar_full[st]), (ch / STAGES) & 1, p.err)) break;
+        tc_fence_after();
+        const uint32_t sa = sbase + st * STAGE_BYTES;
+#pragma unroll
+        for (int G = 0; G < NG; G++) {
+          const uint32_t d = tmem + b * SET_COLS + G * 128;
+#pragma unroll
+          for (int kk = 0; kk < KC / C::KSTEP; kk++) {
+            const uint64_t dh = desc_sw128(sa + G * GROUP_BYTES + kk * 32);
+            const uint64_t dl = desc_sw128(sa + G * GROUP_BYTES + TILE_BYTES + kk * 32);
+            mma_tf32(d, dh, dh, IDESC_TF32, (first && kk == 0) ? 0u : 1u);
+            mma_tf32(d, dl, dh, IDESC_TF32, 1u);
+            mma_tf32(d, dh, dl, IDESC_TF32, 1u);
+          }
+        }
+        mma_commit(smem_u32(&bar_empty[st]));
+        if ((ch % DP) == DP - 1 || ch == nchunks - 1) mma_commit(smem_u32(&bar_ready[b]));
+      }
+      mma_commit(smem_u32(&bar_done));
+      mbar_wait(smem_u32(&bar_done), 0, p.err);  // every issued MMA has finished before TMEM is freed
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue warps
+    const int qd = warp & 3;  // TMEM lane quadrant this warp may access
+    const int row = 32 * qd + lane;
+    const int my_gi = row / R;
+    const int r = row - my_gi * R;
+    const int s1 = r >> 1, part1 = r & 1;
+    const int gi0 = (32 * qd) / R;
+    float2 acc[NG][PP][4];
+#pragma unroll
+    for (int G = 0; G < NG; G++)
+#pragma unroll
+      for (int a = 0; a < PP; a++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[G][a][q] = make_float2(0.f, 0.f);
+    bool ok = true;
+    for (int pd = 0; pd < nper; pd++) {
+      const int b = pd & 1;
+      if (!mbar_wait(smem_u32(&bar_ready[b]), (pd >> 1) & 1, p.err)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+#pragma unroll
+      for (int G = 0; G < NG; G++) {
+#pragma unroll
+        for (int pw = 0; pw < WP; pw++) {
+          const int col = gi0 * R + 16 * pw;
+          float v[16], pv[16];
+          tmem_ld16(tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(b * SET_COLS + G * 128 + col), v);
+#pragma unroll
+          for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
+          // piece pw covers block gi0 + (16*pw)/R, piece index within the block (16*pw % R)/16
+          const bool mine = (gi0 + (16 * pw) / R) == my_gi;
+          const int a = ((16 * pw) % R) / 16;
+#pragma unroll
+          for (int qq = 0; qq < 4; qq++) {
+            const int q = qq + 4 * part1;
+            float re, im;
+            if (part1 == 0) {
+              re = v[2 * q] + pv[2 * q + 1];
+              im = pv[2 * q] - v[2 * q + 1];
+            } else {
+              re = pv[2 * q] + v[2 * q + 1];
+              im = v[2 * q] - pv[2 * q + 1];
+            }
+#pragma unroll
+            for (int aa = 0; aa < PP; aa++) {
+              if (mine && aa == a) {
+                acc[G][aa][qq].x += re;
+                acc[G][aa][qq].y += im;
+              }
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(smem_u32(&bar_drained[b]));
+    }
+    if (ok && s1 < n) {
+      const int j = s1 >> 1, l = s1 & 1;
+#pragma unroll
+      for (int G = 0; G < NG; G++) {
+        const int c = cb + G * GCH + my_gi;
+#pragma unroll
+        for (int a = 0; a < PP; a++) {
+#pragma unroll
+          for (int qq = 0; qq < 4; qq++) {
+            const int s2 = 8 * a + qq + 4 * part1;
+            if (s2 >= n) continue;
+            const int k = s2 >> 1, m = s2 & 1;
+            if (j > k || (j == k && !p.autos)) continue;
+            const int bl = baseline_index(j, k, p.nant);
+            const size_t o = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
+            float2 sm = p.vsum[o], e = p.vcomp[o];
+            two_sum_add(sm.x, e.x, acc[G][a][qq].x);
+            two_sum_add(sm.y, e.y, acc[G][a][qq].y);
+            p.vsum[o] = sm;
+            p.vcomp[o] = e;
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == NPROD_WARPS) tmem_dealloc(tmem, TMEM_COLS);
+}
+
 }  // namespace tc
 
 // two rows (re, im) per stream, two streams per antenna: 4*nant rows must fit one M=128 tile
@@ -464,9 +688,20 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   const size_t smem = (size_t)tc::STAGES * 65536 + 1024;
   static_assert(tc::Cfg<true>::STAGE_BYTES == 65536 && tc::Cfg<false>::STAGE_BYTES == 65536, "stage size");
   if (chan_type == CHAN_F32) {
-    e = cudaFuncSetAttribute(tc::xstage_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto launch = [&](auto kern) -> cudaError_t {
+      cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e2 != cudaSuccess) return e2;
+      kern<<<nchan / p.CS, tc::NTHREADS_SPLIT, smem, s>>>(p);
+      return cudaSuccess;
+    };
+    switch (R) {
+      case 16: e = launch(tc::xstage_tc_split_kernel<16>); break;
+      case 32: e = launch(tc::xstage_tc_split_kernel<32>); break;
+      case 64: e = launch(tc::xstage_tc_split_kernel<64>); break;
+      case 128: e = launch(tc::xstage_tc_split_kernel<128>); break;
+      default: return cudaErrorInvalidValue;
+    }
     if (e != cudaSuccess) return e;
-    tc::xstage_tc_kernel<true><<<nchan / p.CS, tc::NTHREADS, smem, s>>>(p);
   } else {
     e = cudaFuncSetAttribute(tc::xstage_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

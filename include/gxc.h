@@ -50,9 +50,10 @@ enum { GXC_PRECISION_FP32 = 0, GXC_PRECISION_FP16 = 1, GXC_PRECISION_FP8 = 2 };
 enum { GXC_ROTATOR_EXACT = 0, GXC_ROTATOR_FXKERNEL = 1 };
 /* X-stage engine.  TENSOR: tcgen05 MMAs with FP32 accumulation in tensor memory;
  * FP16 data uses kind::f16, FP32 data a hi/lo TF32 split (hi.hi + lo.hi + hi.lo,
- * every product exact, ~2^-20 relative error).  CUDA_CORE: plain FP32 FMAs.
- * AUTO: TENSOR for FP16 data when 4*nant <= 128 and nchan fits its channel tile,
- * CUDA_CORE otherwise (FP32 data stays on round-to-nearest FP32 FMAs). */
+ * every product exact; tensor memory is drained every 128 FFTs, which bounds the
+ * bias of its round-towards-zero accumulation at about 3e-6 relative).
+ * CUDA_CORE: plain FP32 FMAs.  AUTO: TENSOR when 4*nant <= 128 and nchan fits
+ * its channel tile, else CUDA_CORE. */
 enum { GXC_XENGINE_AUTO = 0, GXC_XENGINE_CUDA_CORE = 1, GXC_XENGINE_TENSOR = 2 };
 enum { GXC_LAYOUT_FXKERNEL = 0 };
 

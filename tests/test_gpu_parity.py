@@ -153,7 +153,8 @@ def test_misaligned_device_input_is_rejected_before_any_launch():
     fx.close()
 
 
-@pytest.mark.parametrize("precision,engine,tol", [("fp32", "cuda_core", FP32_TOL), ("fp16", "tensor", FP16_TOL),
+@pytest.mark.parametrize("precision,engine,tol", [("fp32", "cuda_core", FP32_TOL), ("fp32", "tensor", FP32_TOL),
+                                                  ("fp16", "tensor", FP16_TOL),
                                                   ("fp16", "cuda_core", FP16_TOL)])
 def test_long_integration_accuracy_vs_fp64(precision, engine, tol):
     """8192 FFTs accumulated in one block: the accumulation error must stay inside
