@@ -31,6 +31,7 @@ CONFIGS = {
     "c0": ("6 antennas, 2-bit real, 128 Ms/s per pol, 0.25 s, nchan 1024", "config0"),
     "c1": ("16 antennas, 2-bit real, 512 Ms/s per pol, 1.0 s, nchan 4096", "config1"),
     "c2": ("32 antennas, 2-bit real, 1024 Ms/s per pol, 0.5 s, nchan 8192, rho 0.01, tone", "config2"),
+    "c4": ("64 antennas, 8-bit complex, 256 Ms/s per pol, 0.5 s, nchan 32768, rho 0.02", "config4"),
 }
 
 

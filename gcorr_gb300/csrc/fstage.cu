@@ -5,6 +5,7 @@
 // Reference path restated: fxkernel/src/fxkernel.cpp:276-325 (station loop of
 // process()), :425-440 getStationDelay, :443-487 unpack, :498-567 fringerotate,
 // :569-580 dofft, :595-634 fracSampleCorrect.
+#include <cooperative_groups.h>
 #include <math.h>
 #include <stdlib.h>
 #include <vector>
@@ -513,6 +514,204 @@ static cudaError_t launch_fstage_t(const FParams &prm, int nt, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ------------------------------------------------- 32768-point FFT windows
+// One pol of one window is 256 KiB in FP32, more than a CTA's shared memory,
+// so a cluster of two CTAs shares it (four-step factorisation N = 128 x 256):
+//   step 1: CTA r takes columns n2 in [128r, 128r+128): 128-point FFTs over n1
+//           of x[256 n1 + n2] (radix 32 then 4), decoded and fringe-rotated
+//           straight from global memory, times the twiddle W_N^(n2 k1);
+//   step 2: after a cluster barrier, CTA r reads rows k1 in [64r, 64r+64) of
+//           both CTAs' [k1][n2] buffers (half through distributed shared memory);
+//   step 3: after a second cluster barrier, 256-point FFTs over n2 (radix 16 x 16)
+//           give X[k1 + 128 k2], multiplied by the frac-delay phase and stored.
+// The flagged-window path returns before any cluster barrier, in both CTAs alike.
+constexpr int F15 = 32768;
+constexpr int F15_STRIDE = 128;                 // fringe/frac table split (2^floor(log2 nchan / 2))
+constexpr int F15_SUB = F15 / F15_STRIDE;       // 256
+constexpr int F15_BUF = 64 * 272;               // complex slots: max(128x129, 128x132, 64x272)
+
+template <typename OutT, bool CPLX>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_cluster_kernel(FParams prm) {
+  namespace cg = cooperative_groups;
+  constexpr int NCHAN = CPLX ? F15 : F15 / 2;
+  constexpr int FSUB = NCHAN / F15_STRIDE;
+  const Job &job = prm.job;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ float2 smem[];
+  float2 *buf = smem;                       // column, [k1][n2] and row buffers (reused)
+  float2 *tsub = buf + F15_BUF;             // [F15_SUB]
+  float2 *tstep = tsub + F15_SUB;           // [F15_STRIDE]
+  float2 *fsubt = tstep + F15_STRIDE;       // [FSUB]
+  float2 *fstept = fsubt + FSUB;            // [F15_STRIDE]
+  __shared__ Geom g;
+  __shared__ float cst[4];
+
+  const int rk = (int)cluster.block_rank();
+  const int tl = blockIdx.x >> 1;
+  const int ant = blockIdx.y;
+  const int pol = blockIdx.z;
+  const int t = prm.t0 + tl;
+  const int tid = threadIdx.x;
+  const int nstreams = 2 * job.nant;
+  const int s = 2 * ant + pol;
+  OutT *chan = reinterpret_cast<OutT *>(prm.chan);
+  OutT *out0 = chan + ((size_t)tl * nstreams + s) * CW;
+  const size_t ctile_stride = (size_t)prm.T * nstreams * CW;
+  const float2 *__restrict__ tw = prm.tw;
+
+  if (tid == 0) {
+    g = job.geom[(size_t)ant * job.nfft + t];
+    if (g.valid) {
+      const int intdelay = __double2int_rz(g.b);
+      const double br = g.b - (double)intdelay;
+      double c0 = br * job.lo_hz;
+      if (job.fractional_lo) c0 += (job.lo_hz - trunc(job.lo_hz)) * (double)intdelay;
+      c0 -= floor(c0);
+      const double c1 = g.a * job.lo_hz / (double)F15;
+      const double stepmul = (job.rotator == GXC_ROTATOR_FXKERNEL) ? (double)F15_STRIDE : (double)F15_SUB;
+      cst[0] = (float)c0;
+      cst[1] = (float)c1;
+      cst[2] = (float)(c1 * stepmul);
+      cst[3] = (float)(job.bw_hz / (double)NCHAN * g.frac);
+    }
+  }
+  __syncthreads();
+  if (!g.valid) {  // both CTAs of the cluster see the same record
+    const OutT z = to_out<OutT>(make_float2(0.f, 0.f), 1.f);
+    for (int c = rk * (NCHAN / 2) + tid; c < (rk + 1) * (NCHAN / 2); c += 512)
+      out0[(size_t)(c >> 4) * ctile_stride + (c & 15)] = z;
+    return;
+  }
+  {
+    const float c0 = cst[0], c1 = cst[1], cstep = cst[2], cf = cst[3];
+    for (int k = tid; k < F15_SUB; k += 512) {
+      float sn, cs;
+      sincospif(-2.0f * fmaf((float)k, c1, c0), &sn, &cs);
+      tsub[k] = make_float2(cs, sn);
+    }
+    for (int i = tid; i < F15_STRIDE; i += 512) {
+      float sn, cs;
+      sincospif(-2.0f * ((float)i * cstep), &sn, &cs);
+      tstep[i] = make_float2(cs, sn);
+      sincospif(2.0f * ((float)(i * FSUB) * cf), &sn, &cs);
+      fstept[i] = make_float2(cs, sn);
+    }
+    for (int k = tid; k < FSUB; k += 512) {
+      float sn, cs;
+      sincospif(2.0f * ((float)k * cf), &sn, &cs);
+      fsubt[k] = make_float2(cs, sn);
+    }
+  }
+  __syncthreads();
+
+  float2 u[32];
+  // ---- step 1, pass A: radix 32 over n1 = iv + 4 r (sample n = 256 n1 + n2)
+  const int col = tid & 127, iv = tid >> 7;
+  const int n2 = 128 * rk + col;
+  {
+    const uint8_t *in = job.inputs[ant];
+    const long long off = g.offset;
+    const float2 rs = tsub[n2];  // n mod 256 = n2
+    const int shift = 2 * (2 * (int)((off + n2) & 1) + pol);
+#pragma unroll
+    for (int r = 0; r < 32; r++) {
+      const int n1 = iv + 4 * r;
+      const long long m = off + 256LL * n1 + n2;
+      const float2 rot = cmul(rs, tstep[n1]);
+      if constexpr (CPLX) {
+        const char2 x = __ldg(reinterpret_cast<const char2 *>(in + 4 * m + 2 * pol));
+        u[r] = cmul(make_float2((float)x.x, (float)x.y), rot);
+      } else {
+        const int byte = __ldg(in + (m >> 1));
+        const float lv = level2bit((byte >> shift) & 3);
+        u[r] = make_float2(lv * rot.x, lv * rot.y);
+      }
+    }
+    dft<32>(u);
+#pragma unroll
+    for (int r = 0; r < 32; r++) buf[col * 129 + iv * 32 + r] = u[r];
+  }
+  __syncthreads();
+  // ---- step 1, pass B: radix 4 (span 32), then the four-step twiddle W_N^(n2 k1)
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int ivb = iv * 8 + q;
+    float2 *v = &u[4 * q];
+#pragma unroll
+    for (int r = 0; r < 4; r++) v[r] = buf[col * 129 + ivb + 32 * r];
+#pragma unroll
+    for (int r = 1; r < 4; r++) v[r] = cmul(v[r], __ldg(&tw[r * ivb * (F15 / 128)]));
+    dft<4>(v);
+#pragma unroll
+    for (int r = 0; r < 4; r++) v[r] = cmul(v[r], __ldg(&tw[n2 * (ivb + 32 * r)]));
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 8; q++)
+#pragma unroll
+    for (int r = 0; r < 4; r++) buf[(iv * 8 + q + 32 * r) * 132 + col] = u[4 * q + r];
+  cluster.sync();  // both CTAs hold their [k1][n2] halves
+  // ---- step 3, pass C: radix 16 over n2 for rows k1 of this CTA (half the columns remote)
+  const int kr = tid >> 3, t8 = tid & 7;
+  const int k1 = 64 * rk + kr;
+  {
+    const float2 *Y0 = cluster.map_shared_rank(buf, 0);
+    const float2 *Y1 = cluster.map_shared_rank(buf, 1);
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const int ivc = t8 + 8 * q;
+#pragma unroll
+      for (int r = 0; r < 16; r++) {
+        const int nn = ivc + 16 * r;
+        u[16 * q + r] = (r < 8) ? Y0[k1 * 132 + nn] : Y1[k1 * 132 + (nn - 128)];
+      }
+      dft<16>(&u[16 * q]);
+    }
+  }
+  cluster.sync();  // every remote read of this CTA's buffer is done
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int ivc = t8 + 8 * q;
+#pragma unroll
+    for (int r = 0; r < 16; r++) buf[kr * 272 + ivc * 17 + r] = u[16 * q + r];
+  }
+  __syncthreads();
+  // ---- step 3, pass D: radix 16 (span 16); X[k1 + 128 k2], k2 = ivd + 16 r
+  constexpr int RKEEP = CPLX ? 16 : 8;  // real data keeps channels c < N/2
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int ivd = t8 + 8 * q;
+    float2 *v = &u[16 * q];
+#pragma unroll
+    for (int r = 0; r < 16; r++) v[r] = buf[kr * 272 + ivd + 17 * r];
+#pragma unroll
+    for (int r = 1; r < 16; r++) v[r] = cmul(v[r], __ldg(&tw[r * ivd * (F15 / 256)]));
+    dft<16>(v);
+#pragma unroll
+    for (int r = 0; r < RKEEP; r++) {
+      const int c = k1 + 128 * (ivd + 16 * r);
+      const float2 fr = cmul(fsubt[c & (FSUB - 1)], fstept[c / FSUB]);
+      out0[(size_t)(c >> 4) * ctile_stride + (c & 15)] = to_out<OutT>(cmul(v[r], fr), prm.out_scale);
+    }
+  }
+}
+
+template <typename OutT, bool CPLX>
+static cudaError_t launch_fstage_cluster(const FParams &prm, int nt, cudaStream_t s) {
+  const Job &job = prm.job;
+  constexpr int NCHAN = CPLX ? F15 : F15 / 2;
+  if (job.F != F15 || job.nchan != NCHAN || job.stride != F15_STRIDE || job.substride != F15_SUB ||
+      job.fsub != NCHAN / F15_STRIDE)
+    return cudaErrorInvalidValue;
+  const size_t smem = sizeof(float2) * ((size_t)F15_BUF + F15_SUB + 2 * F15_STRIDE + NCHAN / F15_STRIDE);
+  auto kern = fstage_cluster_kernel<OutT, CPLX>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid(2u * (unsigned)nt, (unsigned)job.nant, 2u);
+  kern<<<grid, 512, smem, s>>>(prm);
+  return cudaGetLastError();
+}
+
 template <typename OutT, bool CPLX>
 static cudaError_t launch_fstage_l(const FParams &prm, int nt, cudaStream_t s) {
   switch (prm.job.log2F) {
@@ -523,11 +722,12 @@ static cudaError_t launch_fstage_l(const FParams &prm, int nt, cudaStream_t s) {
     case 12: return launch_fstage_t<12, OutT, CPLX>(prm, nt, s);
     case 13: return launch_fstage_t<13, OutT, CPLX>(prm, nt, s);
     case 14: return launch_fstage_t<14, OutT, CPLX>(prm, nt, s);
+    case 15: return launch_fstage_cluster<OutT, CPLX>(prm, nt, s);
     default: return cudaErrorInvalidValue;
   }
 }
 
-int fstage_supported(int F) { return F >= 256 && F <= 16384 && (F & (F - 1)) == 0; }
+int fstage_supported(int F) { return F >= 256 && F <= 32768 && (F & (F - 1)) == 0; }
 
 static int ilog2(int x) {
   int l = 0;

@@ -110,13 +110,12 @@ std::string validate(const gxc_config *c, gxc_status *st) {
   *st = GXC_ERR_UNSUPPORTED;
   if (!((c->nbit == 2 && !c->is_complex) || (c->nbit == 8 && c->is_complex)))
     return "supported input formats: 2-bit real, 8-bit complex";
-  if (!fstage_supported((int)F)) return "FFT length outside 256..16384";
+  if (!fstage_supported((int)F)) return "FFT length outside 256..32768";
   if (c->precision == GXC_PRECISION_FP8) return "FP8 channelised data is not implemented";
   if (c->x_engine == GXC_XENGINE_TENSOR) {
-    if (!xstage_tensor_supported(c->nant)) return "tensor-core X-stage: needs 4*nant <= 128";
     const int ct = c->precision == GXC_PRECISION_FP32 ? CHAN_F32 : CHAN_F16;
-    if (c->nchan % xstage_tensor_channels_per_cta(c->nant, ct))
-      return "tensor-core X-stage: nchan must be a multiple of its channel tile";
+    if (!xstage_tensor_fits(c->nant, c->nchan, ct))
+      return "tensor-core X-stage: needs nant <= 64 (FP32 data: nant <= 32) and nchan a multiple of its channel tile";
   }
   *st = GXC_OK;
   return "";
@@ -227,24 +226,36 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   // FFTs (TMEM accumulation rounds towards zero; the drains bound that bias at
   // about 3e-6 relative, inside the FP32 tolerance, whatever the integration length).
   if (h->xeng == GXC_XENGINE_AUTO)
-    h->xeng = (xstage_tensor_supported(nant) && cfg->nchan % xstage_tensor_channels_per_cta(nant, h->chan_type) == 0)
-                  ? GXC_XENGINE_TENSOR
-                  : GXC_XENGINE_CUDA_CORE;
+    h->xeng = xstage_tensor_fits(nant, cfg->nchan, h->chan_type) ? GXC_XENGINE_TENSOR : GXC_XENGINE_CUDA_CORE;
   // FP16 storage keeps |X| near the sample rms: scale by 2^-floor(log2(F)/2),
   // an exact power of two undone exactly at finalisation.
   if (h->chan_type == CHAN_F16) {
     h->out_scale = ldexpf(1.0f, -(h->log2F / 2));
     h->vis_scale = ldexpf(1.0f, 2 * (h->log2F / 2));
   }
-  // FFT block: bounded channelised buffer (<= 2 GiB), multiple of 64 FFTs.
+  // FFT block T (FFTs per F/X pass).  Every block adds its partial sums into the
+  // compensated accumulators (read + write of sum and comp), so T is chosen large
+  // enough that this traffic stays under ~6% of the channelised data of a block,
+  // at least 4096 FFTs, and small enough for the device memory budget (40% of
+  // the free memory, leaving room for inputs and the caller).
   const size_t esz = h->chan_type == CHAN_F32 ? sizeof(float2) : sizeof(__half2);
   const size_t per_fft = (size_t)cfg->nchan * 2 * nant * esz;
   int T = cfg->fft_block;
   if (T <= 0) {
-    size_t cap = ((size_t)2 << 30) / per_fft;
+    const size_t nvis_b = (size_t)(h->nbl > 0 ? h->nbl : 1) * 4 * cfg->nchan * sizeof(float2) * 4;
+    size_t want = (16 * nvis_b + per_fft - 1) / per_fft;
+    if (want < 4096) want = 4096;  // fewer, longer X passes amortise each CTA's set-up and epilogue
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      cudaGetLastError();
+      free_b = (size_t)8 << 30;
+    }
+    size_t cap = (size_t)(0.4 * (double)free_b) / per_fft;
     if (cap < 64) cap = 64;
-    T = (int)(cap > (size_t)cfg->nfft ? (size_t)cfg->nfft : cap);
-    if (T > 64) T -= T % 64;
+    size_t tt = want < cap ? want : cap;
+    if (tt > (size_t)cfg->nfft) tt = (size_t)cfg->nfft;
+    T = (int)tt;
+    if (T > 64 && T < cfg->nfft) T -= T % 64;
   }
   if (T > cfg->nfft) T = cfg->nfft;
   h->T = T;

@@ -66,6 +66,7 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
                                  float2 *vsum, float2 *vcomp, cudaStream_t s);
 int xstage_tensor_supported(int nant);
 int xstage_tensor_channels_per_cta(int nant, int chan_type);
+int xstage_tensor_fits(int nant, int nchan, int chan_type);
 cudaError_t xstage_tensor_take_error(int *flag);
 
 // Output baseline index of antennas j <= k (crosses in fxkernel order, then autos).

@@ -105,10 +105,11 @@ gxc_status xcorr_check(int nant, int nfft, int nchan, int fftwidth, int precisio
     return GXC_ERR_UNSUPPORTED;
   }
   const int ct = precision == GXC_PRECISION_FP32 ? CHAN_F32 : CHAN_F16;
-  const bool tc_ok = xstage_tensor_supported(nant) && nchan % xstage_tensor_channels_per_cta(nant, ct) == 0;
+  const bool tc_ok = xstage_tensor_fits(nant, nchan, ct) != 0;
   if (*engine == GXC_XENGINE_AUTO) *engine = tc_ok ? GXC_XENGINE_TENSOR : GXC_XENGINE_CUDA_CORE;
   if (*engine == GXC_XENGINE_TENSOR && !tc_ok) {
-    *msg = "gxc_xcorr: the tensor-core X-stage needs 4*nant <= 128 and nchan a multiple of its channel tile";
+    *msg = "gxc_xcorr: the tensor-core X-stage needs nant <= 64 (FP32 data: nant <= 32) and nchan a multiple of "
+           "its channel tile";
     return GXC_ERR_UNSUPPORTED;
   }
   return GXC_OK;

@@ -212,9 +212,19 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
   const int n = p.nstream;
   const int nchunks = (p.nt + KC - 1) / KC;
 
-  // zero the ring once: rows beyond 2n inside each channel block stay zero
-  for (int i = tid; i < STAGES * STAGE_BYTES / 16; i += NTHREADS)
-    reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
+  // zero the padding rows (2n..R-1 of each channel block) of the ring once; producers never write them
+  if (2 * n < p.R) {
+    const int pad = p.R - 2 * n;
+    const int per_stage = NG * p.g * pad * 8;  // 16-byte words
+    for (int i = tid; i < STAGES * per_stage; i += NTHREADS) {
+      const int st = i / per_stage, r0 = i - st * per_stage;
+      const int w = r0 & 7, rr = r0 >> 3;
+      const int G = rr / (p.g * pad), rem = rr - G * p.g * pad;
+      const int gi = rem / pad, row = gi * p.R + 2 * n + (rem - gi * pad);
+      *reinterpret_cast<uint4 *>(smem + (size_t)st * STAGE_BYTES + G * GROUP_BYTES + row * 128 + w * 16) =
+          make_uint4(0, 0, 0, 0);
+    }
+  }
   if (tid == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(smem_u32(&bar_full[s]), NPROD);
@@ -401,8 +411,18 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
   const int nchunks = (p.nt + KC - 1) / KC;
   const int nper = (nchunks + DP - 1) / DP;
 
-  for (int i = tid; i < STAGES * STAGE_BYTES / 16; i += NTHREADS_SPLIT)
-    reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
+  if (2 * n < R) {  // zero the padding rows of both tiles (hi, lo) of every group of every stage
+    const int pad = R - 2 * n;
+    const int per_stage = NG * GCH * pad * 8 * 2;
+    for (int i = tid; i < STAGES * per_stage; i += NTHREADS_SPLIT) {
+      const int st = i / per_stage, r0 = i - st * per_stage;
+      const int w = r0 & 7, rr = (r0 >> 3) >> 1, tile = (r0 >> 3) & 1;
+      const int G = rr / (GCH * pad), rem = rr - G * GCH * pad;
+      const int gi = rem / pad, row = gi * R + 2 * n + (rem - gi * pad);
+      *reinterpret_cast<uint4 *>(smem + (size_t)st * STAGE_BYTES + G * GROUP_BYTES + tile * TILE_BYTES + row * 128 +
+                                 w * 16) = make_uint4(0, 0, 0, 0);
+    }
+  }
   if (tid == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(smem_u32(&bar_full[s]), NPROD);
@@ -609,10 +629,161 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
   if (warp == NPROD_WARPS) tmem_dealloc(tmem, TMEM_COLS);
 }
 
+
+// FP16 path for 33..64 antennas (R = 256 rows per channel, one channel per CTA).
+// The Gram matrix is split into M-halves: D_top = P[0:128] P^T (N = 256) and
+// D_bot = P[128:256] P[128:256]^T (N = 128); the lower-left block is the
+// transpose of D_top's right half and is not needed (only j <= k is output).
+// 384 of the 512 TMEM columns; one 32 KiB stage per 64 FFTs (4 stages).
+constexpr int BIG_STAGES = 4;
+constexpr int BIG_STAGE_BYTES = 256 * 128;
+constexpr uint32_t IDESC_N256 = (1u << 4) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
+
+__global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big_kernel(Params p) {
+  constexpr int KC = 64;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar_full[BIG_STAGES], bar_empty[BIG_STAGES], bar_done;
+  __shared__ uint32_t tmem_base_sh;
+  unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t sbase = smem_u32(smem);
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int c = blockIdx.x;  // the one channel of this CTA
+  const int n = p.nstream;
+  const int nchunks = (p.nt + KC - 1) / KC;
+
+  if (2 * n < 256) {  // zero the padding rows 2n..255 of every stage
+    const int per_stage = (256 - 2 * n) * 8;
+    for (int i = tid; i < BIG_STAGES * per_stage; i += NTHREADS) {
+      const int st = i / per_stage, r0 = i - st * per_stage;
+      *reinterpret_cast<uint4 *>(smem + (size_t)st * BIG_STAGE_BYTES + (2 * n + (r0 >> 3)) * 128 + (r0 & 7) * 16) =
+          make_uint4(0, 0, 0, 0);
+    }
+  }
+  if (tid == 0) {
+    for (int s = 0; s < BIG_STAGES; s++) {
+      mbar_init(smem_u32(&bar_full[s]), NPROD);
+      mbar_init(smem_u32(&bar_empty[s]), 1);
+    }
+    mbar_init(smem_u32(&bar_done), 1);
+    fence_mbar_init();
+  }
+  if (warp == NPROD_WARPS) {
+    tmem_alloc(smem_u32(&tmem_base_sh), 512);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+
+  if (warp < NPROD_WARPS) {
+    // task = (stream s, 16-byte K chunk o): 8 FFTs of one stream of this channel
+    const int ntask = 8 * n;
+    const __half2 *src = (const __half2 *)p.chan + ((size_t)(c >> 4) * p.T * n) * CW + (c & 15);
+    for (int ch = 0; ch < nchunks; ch++) {
+      const int st = ch % BIG_STAGES;
+      if (ch >= BIG_STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / BIG_STAGES) - 1) & 1, p.err)) break;
+      unsigned char *stage = smem + (size_t)st * BIG_STAGE_BYTES;
+      const int tb = ch * KC;
+      for (int task = tid; task < ntask; task += NPROD) {
+        const int s = task % n;
+        const int o = task / n;
+        uint32_t w[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const int t = tb + 8 * o + i;
+          w[i] = (t < p.nt) ? __ldg(reinterpret_cast<const uint32_t *>(src + ((size_t)t * n + s) * CW)) : 0u;
+        }
+        const uint4 re = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410), prmt(w[4], w[5], 0x5410),
+                                    prmt(w[6], w[7], 0x5410));
+        const uint4 im = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632), prmt(w[4], w[5], 0x7632),
+                                    prmt(w[6], w[7], 0x7632));
+        const int row = 2 * s;
+        *reinterpret_cast<uint4 *>(stage + row * 128 + ((o ^ (row & 7)) << 4)) = re;
+        *reinterpret_cast<uint4 *>(stage + (row + 1) * 128 + ((o ^ ((row + 1) & 7)) << 4)) = im;
+      }
+      fence_proxy_async_smem();
+      mbar_arrive(smem_u32(&bar_full[st]));
+    }
+  } else if (lane == 0) {
+    for (int ch = 0; ch < nchunks; ch++) {
+      const int st = ch % BIG_STAGES;
+      if (!mbar_wait(smem_u32(&bar_full[st]), (ch / BIG_STAGES) & 1, p.err)) break;
+      tc_fence_after();
+      const uint32_t sa = sbase + st * BIG_STAGE_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < KC / 16; kk++) {
+        const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
+        const uint64_t dall = desc_sw128(sa + kk * 32);            // rows 0..255 (also the top half's A)
+        const uint64_t dbot = desc_sw128(sa + 128 * 128 + kk * 32);  // rows 128..255
+        mma_f16(tmem, dall, dall, IDESC_N256, acc);                // D_top: rows 0..127 x cols 0..255
+        mma_f16(tmem + 256, dbot, dbot, IDESC, acc);               // D_bot: rows 128..255 x cols 128..255
+      }
+      mma_commit(smem_u32(&bar_empty[st]));
+    }
+    mma_commit(smem_u32(&bar_done));
+    mbar_wait(smem_u32(&bar_done), 0, p.err);
+  }
+
+  if (warp < 4) {
+    const bool ok = mbar_wait(smem_u32(&bar_done), 0, p.err);
+    tc_fence_after();
+    if (ok) {
+      // half 0: TMEM lane = row a (0..127), columns 0..255;  half 1: lane = row 128 + a, columns 128..255
+      for (int half = 0; half < 2; half++) {
+        const int arow = 128 * half + 32 * warp + lane;
+        const int s1 = arow >> 1, part1 = arow & 1;
+        const int j = s1 >> 1, l = s1 & 1;
+        const int npc = half ? 8 : 16;
+        for (int pc = 0; pc < npc; pc++) {
+          __syncwarp();
+          float v[16], pv[16];
+          const uint32_t col = half ? (256u + 16u * pc) : (16u * pc);
+          tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + col, v);
+#pragma unroll
+          for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
+          if (s1 >= n) continue;
+          const int s2b = (half ? 64 : 0) + 8 * pc;
+#pragma unroll
+          for (int qq = 0; qq < 4; qq++) {
+            const int q = qq + 4 * part1;
+            const int s2 = s2b + q;
+            if (s2 >= n) continue;
+            const int k = s2 >> 1, m = s2 & 1;
+            if (j > k || (j == k && !p.autos)) continue;
+            float re, im;
+            if (part1 == 0) {
+              re = v[2 * q] + pv[2 * q + 1];
+              im = pv[2 * q] - v[2 * q + 1];
+            } else {
+              re = pv[2 * q] + v[2 * q + 1];
+              im = v[2 * q] - pv[2 * q + 1];
+            }
+            const int bl = baseline_index(j, k, p.nant);
+            const size_t o = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
+            float2 sm = p.vsum[o], e = p.vcomp[o];
+            two_sum_add(sm.x, e.x, re);
+            two_sum_add(sm.y, e.y, im);
+            p.vsum[o] = sm;
+            p.vcomp[o] = e;
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == NPROD_WARPS) tmem_dealloc(tmem, 512);
+}
+
 }  // namespace tc
 
-// two rows (re, im) per stream, two streams per antenna: 4*nant rows must fit one M=128 tile
-int xstage_tensor_supported(int nant) { return nant >= 1 && 4 * nant <= 128; }
+// two rows (re, im) per stream, two streams per antenna: up to 32 antennas fill one
+// M = 128 tile per channel; 33..64 antennas use the split-M kernel (FP16 only)
+int xstage_tensor_supported(int nant) { return nant >= 1 && 4 * nant <= 256; }
 
 static int g_err_dev = -1;
 static int *g_err = nullptr;
@@ -645,9 +816,17 @@ cudaError_t xstage_tensor_take_error(int *flag) {
 
 // Channels per CTA of the tensor-core X-stage for nant antennas (the channel count must divide by it).
 int xstage_tensor_channels_per_cta(int nant, int chan_type) {
+  if (4 * nant > 128) return chan_type == CHAN_F32 ? 0 : 1;  // split-M kernel: one channel, FP16 only
   int R = 16;
   while (R < 4 * nant) R <<= 1;  // 2 rows (re, im) per stream, 2 streams per antenna
   return (chan_type == CHAN_F32 ? tc::Cfg<true>::NG : tc::Cfg<false>::NG) * (128 / R);
+}
+
+// True when the tensor-core X-stage can run this shape.
+int xstage_tensor_fits(int nant, int nchan, int chan_type) {
+  if (!xstage_tensor_supported(nant)) return 0;
+  const int cs = xstage_tensor_channels_per_cta(nant, chan_type);
+  return cs > 0 && nchan % cs == 0;
 }
 
 cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,
@@ -665,16 +844,21 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   int R = 16;
   while (R < 2 * p.nstream) R <<= 1;  // 2 rows (re, im) per stream
   p.R = R;
-  p.g = 128 / R;
+  p.g = R <= 128 ? 128 / R : 1;
   p.CS = xstage_tensor_channels_per_cta(nant, chan_type);
-  if (nchan % p.CS) return cudaErrorInvalidValue;
+  if (p.CS <= 0 || nchan % p.CS) return cudaErrorInvalidValue;
   p.vsum = vsum;
   p.vcomp = vcomp;
   cudaError_t e = xstage_tensor_error_flag(&p.err);
   if (e != cudaSuccess) return e;
   const size_t smem = (size_t)tc::STAGES * 65536 + 1024;
   static_assert(tc::Cfg<true>::STAGE_BYTES == 65536 && tc::Cfg<false>::STAGE_BYTES == 65536, "stage size");
-  if (chan_type == CHAN_F32) {
+  if (R > 128) {
+    const size_t bsmem = (size_t)tc::BIG_STAGES * tc::BIG_STAGE_BYTES + 1024;
+    e = cudaFuncSetAttribute(tc::xstage_tc_big_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
+    if (e != cudaSuccess) return e;
+    tc::xstage_tc_big_kernel<<<nchan, tc::NTHREADS, bsmem, s>>>(p);
+  } else if (chan_type == CHAN_F32) {
     auto launch = [&](auto kern) -> cudaError_t {
       cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e2 != cudaSuccess) return e2;

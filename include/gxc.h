@@ -52,8 +52,8 @@ enum { GXC_ROTATOR_EXACT = 0, GXC_ROTATOR_FXKERNEL = 1 };
  * FP16 data uses kind::f16, FP32 data a hi/lo TF32 split (hi.hi + lo.hi + hi.lo,
  * every product exact; tensor memory is drained every 128 FFTs, which bounds the
  * bias of its round-towards-zero accumulation at about 3e-6 relative).
- * CUDA_CORE: plain FP32 FMAs.  AUTO: TENSOR when 4*nant <= 128 and nchan fits
- * its channel tile, else CUDA_CORE. */
+ * TENSOR covers up to 64 antennas with FP16 data and up to 32 with FP32 data.
+ * CUDA_CORE: plain FP32 FMAs.  AUTO: TENSOR when the shape fits, else CUDA_CORE. */
 enum { GXC_XENGINE_AUTO = 0, GXC_XENGINE_CUDA_CORE = 1, GXC_XENGINE_TENSOR = 2 };
 enum { GXC_LAYOUT_FXKERNEL = 0 };
 

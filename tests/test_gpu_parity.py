@@ -59,10 +59,11 @@ def test_golden_exact_mode_matches_fp64_oracle(golden_cases, engine):
 
 
 @pytest.mark.parametrize("nchan,is_complex", [(128, False), (256, False), (512, False), (1024, False),
-                                              (2048, False), (4096, False), (8192, False),
-                                              (256, True), (1024, True), (4096, True), (16384, True)])
+                                              (2048, False), (4096, False), (8192, False), (16384, False),
+                                              (256, True), (1024, True), (4096, True), (16384, True),
+                                              (32768, True)])
 def test_fft_sizes_vs_fp64(nchan, is_complex):
-    nfft = 6 if nchan * (1 if is_complex else 2) >= 8192 else 12
+    nfft = 4 if nchan * (1 if is_complex else 2) >= 32768 else 6 if nchan * (1 if is_complex else 2) >= 8192 else 12
     w = synth.Workload(nant=2, nchan=nchan, nfft=nfft, nbit=8 if is_complex else 2, is_complex=is_complex,
                        bw_hz=64e6, seed=nchan + is_complex, offset_us=0.5)
     d = synth.random_bytes(w)

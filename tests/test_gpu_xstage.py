@@ -20,6 +20,8 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 KAT_SHAPES = [(3, 512, 256, 4), (5, 1024, 1024, 100), (3, 1024, 512, 3000)]
+# beyond the reference's shapes: 33..64 antennas (split-M tensor kernel)
+BIG_KAT = (48, 256, 128, 70)
 
 
 def cint_data(n, seed=12345):
@@ -66,7 +68,7 @@ def test_xstage_known_answer_exact(shape, name, prec, eng):
     assert np.array_equal(got, exp), (name, np.abs(got - exp).max())
 
 
-@pytest.mark.parametrize("nant", [1, 2, 4, 7, 8, 16, 32])
+@pytest.mark.parametrize("nant", [1, 2, 4, 7, 8, 16, 32, 33, 48, 64])
 def test_tensor_vs_cuda_core_with_autos(nant):
     nchan, fftwidth, nfft = 128, 256, 300
     rng = np.random.default_rng(nant)
@@ -121,3 +123,13 @@ def test_tensor_split_fp32_matches_cuda_core_fp32(nant):
     ref = expected_crosscorraccum(data, nant, nfft, nchan, fftwidth, autos=True)
     assert O.rel_rms_per_product(a, ref).max() < 1e-5
     assert O.rel_rms_per_product(b, ref).max() < 1e-5
+
+
+@pytest.mark.parametrize("name,prec,eng", [("fp32-cuda-core", L.GXC_PRECISION_FP32, L.GXC_XENGINE_CUDA_CORE),
+                                           ("fp16-tensor", L.GXC_PRECISION_FP16, L.GXC_XENGINE_TENSOR)])
+def test_xstage_known_answer_exact_many_antennas(name, prec, eng):
+    nant, fftwidth, nchan, nfft = BIG_KAT
+    data = cint_data(2 * nant * fftwidth * nfft, seed=77)
+    exp = expected_crosscorraccum(data, nant, nfft, nchan, fftwidth, autos=True).astype(np.complex64)
+    got = xcorr(data, nant, nfft, nchan, fftwidth, prec, eng, autos=True)
+    assert np.array_equal(got, exp), (name, np.abs(got - exp).max())
