@@ -31,6 +31,8 @@ CONFIGS = {
     "c0": ("6 antennas, 2-bit real, 128 Ms/s per pol, 0.25 s, nchan 1024", "config0"),
     "c1": ("16 antennas, 2-bit real, 512 Ms/s per pol, 1.0 s, nchan 4096", "config1"),
     "c2": ("32 antennas, 2-bit real, 1024 Ms/s per pol, 0.5 s, nchan 8192, rho 0.01, tone", "config2"),
+    "c3": ("8 uneven jobs (nant 4-24, nchan 256-16384, 2-bit real / 8-bit complex, 64-512 Ms/s, 0.1-0.5 s) "
+           "in one graph launch", "config3_jobs"),
     "c4": ("64 antennas, 8-bit complex, 256 Ms/s per pol, 0.5 s, nchan 32768, rho 0.02", "config4"),
 }
 
@@ -174,6 +176,35 @@ def cpu_sample(w, budget_s: float = 12.0):
                       f"{nthreads} threads), {dt:.1f} s", "seconds": dt}
 
 
+def port_plan(ws, budget_s: float, nthreads: int):
+    """Bounded sample of a list of jobs: the same fraction of every job's FFTs, sized so
+    one pass of the FP32 port over all of them takes about budget_s on nthreads threads."""
+    cal = []
+    for w in ws:
+        n0 = max(1, min(w.nfft, nthreads))
+        _, dt, seed = cpu_port_run(w, n0, nthreads)
+        cal.append((w, dt / n0, seed))
+    full = sum(per * w.nfft for w, per, _ in cal)
+    frac = min(1.0, budget_s / max(full, 1e-9))
+    plan = []
+    for w, per, _ in cal:
+        n = int(max(min(w.nfft, nthreads), min(w.nfft, round(frac * w.nfft))))
+        n -= n % nthreads if n > nthreads else 0
+        _, _, seed = cpu_port_run(w, n, nthreads)
+        plan.append((w, n, seed))
+    return plan
+
+
+def run_plan(plan, nthreads):
+    t = 0.0
+    samples = 0
+    for w, n, seed in plan:
+        _, dt, _ = cpu_port_run(w, n, nthreads, seed)
+        t += dt
+        samples += w.nant * 2 * n * w.fft_len
+    return samples, t
+
+
 def run_reference_arm(args):
     rank, world, local = dist_env()
     if world > 1:
@@ -182,34 +213,149 @@ def run_reference_arm(args):
             barrier(world)
             return
     w = workload(args.config)
+    ws = w if isinstance(w, list) else [w]
     nthreads = os.cpu_count() or 1
-    # one step = the port on a bounded FFT sample (about args.ref_step_s of CPU time)
-    rate, dt, seed = cpu_port_run(w, nthreads, nthreads)
-    n = int(max(nthreads, min(w.nfft, args.ref_step_s / max(dt / nthreads, 1e-6))))
-    n -= n % nthreads if n > nthreads else 0
-    rate, dt, seed = cpu_port_run(w, n, nthreads)
+    # one step = the port over a bounded FFT sample of every job (about args.ref_step_s of CPU time)
+    plan = port_plan(ws, args.ref_step_s, nthreads)
     for _ in range(args.warmup):
-        cpu_port_run(w, n, nthreads, seed)
-    times = []
+        run_plan(plan, nthreads)
+    tot = 0.0
+    samples = 0
     for _ in range(args.steps):
-        r, dt, _ = cpu_port_run(w, n, nthreads, seed)
-        times.append(dt)
-    tot = sum(times)
-    samples = w.nant * 2 * n * w.fft_len * args.steps
+        s_, t_ = run_plan(plan, nthreads)
+        tot += t_
+        samples += s_
     val = samples / tot / 1e9
+    sample = "; ".join(f"{n} of {j.nfft} FFTs" for j, n, _ in plan)
     line = {"impl": "reference", "metric": "input Gsamples/s", "value": val, "unit": "input Gsamples/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": CONFIGS[args.config][0], "sample_ffts_per_step": n, "nfft": w.nfft,
-                       "parallelism": "host threads"},
+            "config": {"workload": CONFIGS[args.config][0], "sample_ffts_per_step": [n for _, n, _ in plan],
+                       "nfft": [j.nfft for j in ws], "parallelism": "host threads"},
             "cpu_baseline": {"value": val, "unit": "input Gsamples/s", "cores": nthreads, "kind": "port",
-                             "sample": f"{n} of {w.nfft} FFTs per step, FP32 port of fxkernel (oracle/fxoracle.c), "
+                             "sample": f"{sample} per step, FP32 port of fxkernel (oracle/fxoracle.c), "
                                        f"{nthreads} threads (IPP unavailable)"},
             "e2e": {"value": val, "unit": "input Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     if world > 1:
         barrier(world)
+
+
+def run_batch_bench(args):
+    """Config 3: eight uneven jobs, autotuned per shape, as one graph launch per step."""
+    import numpy as np
+    import torch
+    from gcorr_gb300 import synth
+    from gcorr_gb300.autotune import tune
+    from gcorr_gb300.batch import Batch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    init_dist(world, "nccl")
+    dev = torch.device("cuda", local)
+    ws = synth.config3_jobs(seed=3 + 1000 * rank)
+    tg = time.perf_counter()
+    data = [synth.generate(w, device=dev) for w in ws]
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - tg
+    base = []
+    for w, d in zip(ws, data):
+        base.append(dict(nant=w.nant, nchan=w.nchan, nfft=w.nfft, nbit=w.nbit, lo=w.lo_hz, bw=w.bw_hz,
+                         is_complex=w.is_complex, inputs=d["inputs"], poly=d["poly"], fso=d["fso"], autos=True))
+    prec = args.precision if args.precision != "fp32" else "fp16"
+    tuned = [tune(dict(b, precision=prec)) for b in base]
+    jobs16 = [dict(b, precision=prec, x_engine=t["x_engine"], fft_block=t["fft_block"]) for b, t in zip(base, tuned)]
+    jobs32 = [dict(b, precision="fp32", x_engine="cuda_core") for b in base]
+    samples = sum(w.input_samples for w in ws)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+
+    def timed(batch, k):
+        for _ in range(args.warmup):
+            batch.launch(sptr)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            batch.launch(sptr)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    b16 = Batch(jobs16)
+    os.makedirs(args.out_dir, exist_ok=True)
+    clk = ClockSampler(local, os.path.join(args.out_dir, f"clocks_r{rank}.csv"))
+    barrier(world)
+    with clk:
+        time.sleep(0.3)
+        ms = timed(b16, args.steps)
+    ms_max = reduce_max(ms, world, dev)
+    launches = b16.launches
+    vis16 = [b16.visibilities(i) for i in range(len(ws))]
+    b32 = Batch(jobs32)
+    ms32 = timed(b32, max(1, args.steps // 2))
+    vis32 = [b32.visibilities(i) for i in range(len(ws))]
+    b32.close()
+    err = [float(np.sqrt(np.sum(np.abs(a - b) ** 2) / max(np.sum(np.abs(b) ** 2), 1e-30))) for a, b in zip(vis16, vis32)]
+
+    # e2e: host->device copies of every job's input, the graph launch, device->host of every result
+    e2e = None
+    if not args.no_e2e:
+        host = [[x.cpu().pin_memory() for x in d["inputs"]] for d in data]
+        outs = [torch.empty((b16.shapes[i][0] * 4 * b16.shapes[i][1],), dtype=torch.complex64).pin_memory()
+                for i in range(len(ws))]
+        import ctypes as C
+        from gcorr_gb300 import _lib as L
+
+        def e2e_step():
+            with torch.cuda.stream(stream):
+                for hx, d in zip(host, data):
+                    for hbuf, dbuf in zip(hx, d["inputs"]):
+                        dbuf.copy_(hbuf, non_blocking=True)
+            b16.launch(sptr)
+            stream.synchronize()
+            for i in range(len(ws)):
+                h = b16.handle(i)
+                L.check(L.lib().gxc_get_visibilities(h, C.c_void_p(outs[i].data_ptr())), h, "get")
+
+        for _ in range(args.warmup):
+            e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        ems = (time.perf_counter() - t0) / args.steps * 1e3
+        ems = reduce_max(ems, world, dev)
+        e2e = {"value": samples * world / (ems / 1e3) / 1e9, "unit": "input Gsamples/s",
+               "h2d_bytes_per_step": int(sum(x.numel() for hx in host for x in hx)),
+               "d2h_bytes_per_step": int(sum(o.numel() * 8 for o in outs)), "ms_per_step": ems}
+    b16.close()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        plan = port_plan(ws, 12.0, nthreads)
+        cs, ct = run_plan(plan, nthreads)
+        cpu = {"value": cs / ct / 1e9, "unit": "input Gsamples/s", "cores": nthreads, "kind": "port",
+               "sample": "; ".join(f"{n} of {j.nfft} FFTs" for j, n, _ in plan)
+                         + f" (random bytes, FP32 port of fxkernel, {nthreads} threads), {ct:.1f} s"}
+    if rank == 0:
+        pk = peaks()
+        line = {
+            "metric": "input Gsamples/s", "value": samples * world / (ms_max / 1e3) / 1e9, "unit": "input Gsamples/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16", "data": "synthetic",
+            "config": {"workload": CONFIGS["c3"][0], "parallelism": f"replicas x{world}",
+                       "jobs": [{"nant": w.nant, "nchan": w.nchan, "nfft": w.nfft, "nbit": w.nbit,
+                                 "complex": w.is_complex, "x_engine": t["x_engine"], "fft_block": t["fft_block"]}
+                                for w, t in zip(ws, tuned)],
+                       "l2": f"inputs larger than L2 ({sum(w.bytes_per_antenna * w.nant for w in ws) / 1e9:.1f} GB)"},
+            "fp32_cuda_core_batch_ms": ms32, "speedup_vs_fp32_cuda_core_batch": ms32 / ms,
+            "fp16_vs_fp32_rel_rms_per_job": err, "gpu_launches": launches * args.steps,
+            "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cpu, "generator_s": gen_s,
+            "roofline": None, "peak_source": pk["source"],
+        }
+        print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------- GPU side
@@ -234,6 +380,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.config == "c3":
+        return run_batch_bench(args)
 
     import numpy as np
     import torch

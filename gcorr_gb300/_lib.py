@@ -26,7 +26,8 @@ EXPORTS = [
     "gxc_status_string", "gxc_create", "gxc_destroy", "gxc_set_input", "gxc_set_delays", "gxc_process",
     "gxc_sync", "gxc_accumulate", "gxc_get_visibilities", "gxc_device_visibilities", "gxc_get_baseline_counts",
     "gxc_get_valid_flags", "gxc_last_error", "gxc_last_launch_count", "gxc_fft_block", "gxc_enable_stage_timing",
-    "gxc_stage_times", "gxc_xcorr", "gxc_xcorr_noalloc",
+    "gxc_stage_times", "gxc_xcorr", "gxc_xcorr_noalloc", "gxc_batch_create", "gxc_batch_launch", "gxc_batch_size",
+    "gxc_batch_job", "gxc_batch_launch_count", "gxc_batch_destroy",
 ]
 
 
@@ -35,6 +36,10 @@ class GxcConfig(C.Structure):
                 ("is_complex", C.c_int), ("lo_hz", C.c_double), ("bw_hz", C.c_double), ("precision", C.c_int),
                 ("rotator", C.c_int), ("autos", C.c_int), ("x_engine", C.c_int), ("fft_block", C.c_int),
                 ("device", C.c_int)]
+
+
+class GxcJob(C.Structure):
+    _fields_ = [("cfg", GxcConfig), ("inputs", C.c_void_p), ("poly", C.c_void_p), ("fso", C.c_void_p)]
 
 
 class GxcError(RuntimeError):
@@ -104,6 +109,18 @@ def lib():
         l.gxc_xcorr.restype = C.c_int
         l.gxc_xcorr_noalloc.argtypes = [V, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, V, V]
         l.gxc_xcorr_noalloc.restype = C.c_int
+        l.gxc_batch_create.argtypes = [V, C.c_int, P(V)]
+        l.gxc_batch_create.restype = C.c_int
+        l.gxc_batch_launch.argtypes = [V, V]
+        l.gxc_batch_launch.restype = C.c_int
+        l.gxc_batch_size.argtypes = [V]
+        l.gxc_batch_size.restype = C.c_int
+        l.gxc_batch_job.argtypes = [V, C.c_int]
+        l.gxc_batch_job.restype = V
+        l.gxc_batch_launch_count.argtypes = [V]
+        l.gxc_batch_launch_count.restype = C.c_int
+        l.gxc_batch_destroy.argtypes = [V]
+        l.gxc_batch_destroy.restype = C.c_int
         _lib = l
     return _lib
 

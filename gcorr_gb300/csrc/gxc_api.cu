@@ -45,6 +45,7 @@ struct gxc_handle {
   int32_t *d_counts = nullptr;
   uint8_t *d_valid = nullptr;
   float2 *d_tw = nullptr;
+  int2 *d_pairs = nullptr;  // tile pairs of the CUDA-core X-stage
   void *d_chan = nullptr;
   float2 *d_vsum = nullptr, *d_vcomp = nullptr, *d_vis = nullptr;
   cudaStream_t last_stream = nullptr;
@@ -182,6 +183,7 @@ static void release(gxc_handle *h) {
   cudaFree(h->d_counts);
   cudaFree(h->d_valid);
   cudaFree(h->d_tw);
+  cudaFree(h->d_pairs);
   cudaFree(h->d_chan);
   cudaFree(h->d_vsum);
   cudaFree(h->d_vcomp);
@@ -298,6 +300,7 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   A((void **)&h->d_vcomp, sizeof(float2) * nvis);
   A((void **)&h->d_vis, sizeof(float2) * nvis);
   if (e == cudaSuccess) e = make_twiddles(h->F, &h->d_tw);
+  if (e == cudaSuccess) e = make_tile_pairs(nant, &h->d_pairs);
   h->stage_bytes = sizeof(uint8_t *) * nant + sizeof(double) * 4 * nant;
   if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_stage, h->stage_bytes);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_upload, cudaEventDisableTiming);
@@ -406,8 +409,16 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
   const int nant = c.nant;
   int launches = 0;
 
-  // upload pointers + delay model through pinned staging (wait for the previous upload)
-  GXC_CUDA(h, cudaEventSynchronize(h->ev_upload), "waiting for the previous upload");
+  // upload pointers + delay model through pinned staging (wait for the previous upload;
+  // not while the stream is being captured into a graph, whose replays reuse the staging)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  GXC_CUDA(h, cudaStreamIsCapturing(s, &cap), "querying stream capture");
+  const bool capturing = cap != cudaStreamCaptureStatusNone;
+  if (!capturing) GXC_CUDA(h, cudaEventSynchronize(h->ev_upload), "waiting for the previous upload");
+  // inside a capture the handle's events become graph nodes that record on every replay,
+  // so sync() and the getters wait for the latest graph launch; stage timing is off there
+  const unsigned rec_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  const bool timing = h->stage_timing && !capturing;
   const uint8_t **sp = (const uint8_t **)h->h_stage;
   double *spoly = (double *)(h->h_stage + sizeof(uint8_t *) * nant);
   double *sfso = spoly + 3 * nant;
@@ -421,7 +432,7 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
            "uploading delays");
   GXC_CUDA(h, cudaMemcpyAsync(h->d_fso, sfso, sizeof(double) * nant, cudaMemcpyHostToDevice, s),
            "uploading file start offsets");
-  GXC_CUDA(h, cudaEventRecord(h->ev_upload, s), "recording the upload event");
+  GXC_CUDA(h, cudaEventRecordWithFlags(h->ev_upload, s, rec_flags), "recording the upload event");
   if (h->input_on_host) {
     for (int a = 0; a < nant; a++)
       GXC_CUDA(h,
@@ -429,7 +440,7 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
                                cudaMemcpyHostToDevice, s),
                "copying input to the device");
   }
-  if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_begin, s), "timing event");
+  if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_begin, s), "timing event");
 
   GXC_CUDA(h, launch_geometry(h->job, s), "geometry kernel");
   launches++;
@@ -441,7 +452,7 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
   GXC_CUDA(h, cudaMemsetAsync(h->d_vsum, 0, sizeof(float2) * nvis, s), "clearing accumulators");
   GXC_CUDA(h, cudaMemsetAsync(h->d_vcomp, 0, sizeof(float2) * nvis, s), "clearing accumulators");
 
-  if (h->stage_timing && h->ev_stage.size() != (size_t)3 * h->nblocks) {
+  if (timing && h->ev_stage.size() != (size_t)3 * h->nblocks) {
     for (cudaEvent_t e : h->ev_stage) cudaEventDestroy(e);
     h->ev_stage.assign((size_t)3 * h->nblocks, nullptr);
     for (auto &e : h->ev_stage) GXC_CUDA(h, cudaEventCreate(&e), "timing event");
@@ -449,11 +460,11 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
   for (int b = 0; b < h->nblocks; b++) {
     const int t0 = b * h->T;
     const int nt = (c.nfft - t0) < h->T ? (c.nfft - t0) : h->T;
-    if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b], s), "timing event");
+    if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b], s), "timing event");
     GXC_CUDA(h, launch_fstage(h->job, h->d_tw, t0, nt, h->T, h->d_chan, h->chan_type, h->out_scale, s),
              "F-stage kernel");
     launches++;
-    if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b + 1], s), "timing event");
+    if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b + 1], s), "timing event");
     if (h->nbl > 0) {
       if (h->xeng == GXC_XENGINE_TENSOR) {
         GXC_CUDA(h,
@@ -462,13 +473,13 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
                  "tensor-core X-stage kernel");
       } else {
         GXC_CUDA(h,
-                 launch_xstage_cuda_core(h->d_chan, h->chan_type, nant, c.nchan, h->T, nt, c.autos, h->d_vsum,
-                                         h->d_vcomp, s),
+                 launch_xstage_cuda_core(h->d_chan, h->chan_type, nant, c.nchan, h->T, nt, c.autos, h->d_pairs,
+                                         h->d_vsum, h->d_vcomp, s),
                  "X-stage kernel");
       }
       launches++;
     }
-    if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b + 2], s), "timing event");
+    if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b + 2], s), "timing event");
   }
   if (nvis > 0) {
     const int th = 256;
@@ -477,9 +488,9 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
     GXC_CUDA(h, cudaGetLastError(), "finalize kernel");
     launches++;
   }
-  if (h->stage_timing) GXC_CUDA(h, cudaEventRecord(h->ev_end, s), "timing event");
-  GXC_CUDA(h, cudaEventRecord(h->ev_done, s), "recording the completion event");
-  h->last_stream = s;
+  if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_end, s), "timing event");
+  GXC_CUDA(h, cudaEventRecordWithFlags(h->ev_done, s, rec_flags), "recording the completion event");
+  if (!capturing) h->last_stream = s;
   h->processed = true;
   h->launches = launches;
   return GXC_OK;

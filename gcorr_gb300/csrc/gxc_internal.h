@@ -54,7 +54,9 @@ int fstage_supported(int F);
 // xstage_fp32.cu: accumulates visibilities of FFTs [0, nt) of the block into
 // the compensated (sum, comp) accumulators in the output layout.
 cudaError_t launch_xstage_cuda_core(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,
-                                    float2 *vsum, float2 *vcomp, cudaStream_t s);
+                                    const int2 *pairs, float2 *vsum, float2 *vcomp, cudaStream_t s);
+// Device table of (J, K) 2-antenna tile pairs, J <= K, J-major (cudaMalloc'd; caller frees).
+cudaError_t make_tile_pairs(int nant, int2 **out);
 
 cudaError_t launch_xstage_cuda_core_pairs(const void *chan, int chan_type, int nant, int nchan, int T, int nt,
                                           int autos, const int2 *pairs, float2 *vsum, float2 *vcomp,

@@ -60,8 +60,8 @@ namespace gxc {
 //   chan: block buffer of T*nstream*nchan elements (float2 or half2),
 //   vsum, vcomp: nbl*4*nchan float2 each.
 gxc_status xcorr_run(const float2 *ants, int nant, int nfft, int nchan, int fftwidth, int precision, int engine,
-                     int autos, float2 *out, void *chan, int T, float2 *vsum, float2 *vcomp, cudaStream_t s,
-                     std::string *msg) {
+                     int autos, float2 *out, void *chan, int T, const int2 *pairs, float2 *vsum, float2 *vcomp,
+                     cudaStream_t s, std::string *msg) {
   const int nstream = 2 * nant;
   const int nbl = nant * (nant - 1) / 2 + (autos ? nant : 0);
   const size_t nvis = (size_t)nbl * 4 * nchan;
@@ -82,7 +82,7 @@ gxc_status xcorr_run(const float2 *ants, int nant, int nfft, int nchan, int fftw
     if (engine == GXC_XENGINE_TENSOR)
       e = launch_xstage_tensor(chan, ct, nant, nchan, T, nt, autos, vsum, vcomp, s);
     else
-      e = launch_xstage_cuda_core(chan, ct, nant, nchan, T, nt, autos, vsum, vcomp, s);
+      e = launch_xstage_cuda_core(chan, ct, nant, nchan, T, nt, autos, pairs, vsum, vcomp, s);
   }
   if (e == cudaSuccess && nvis) {
     divide_kernel<<<(unsigned)((nvis + 255) / 256), 256, 0, s>>>(vsum, vcomp, nvis, (float)nfft, out);
@@ -136,8 +136,10 @@ extern "C" gxc_status gxc_xcorr(const float *ants, int nant, int nfft, int nchan
   // scratch: channelised block, accumulators, device copies of host buffers
   void *chan = nullptr;
   float2 *vsum = nullptr, *vcomp = nullptr, *dants = nullptr, *dout = nullptr;
+  int2 *pairs = nullptr;
   const bool ants_dev = is_device(ants), out_dev = is_device(accum);
   cudaError_t e = cudaMalloc(&chan, (size_t)T * 2 * nant * nchan * esz);
+  if (e == cudaSuccess) e = make_tile_pairs(nant, &pairs);
   if (e == cudaSuccess) e = cudaMalloc((void **)&vsum, nvis * sizeof(float2) + 16);
   if (e == cudaSuccess) e = cudaMalloc((void **)&vcomp, nvis * sizeof(float2) + 16);
   if (e == cudaSuccess && !ants_dev) e = cudaMalloc((void **)&dants, nin * sizeof(float2));
@@ -145,7 +147,7 @@ extern "C" gxc_status gxc_xcorr(const float *ants, int nant, int nfft, int nchan
   if (e == cudaSuccess && !ants_dev) e = cudaMemcpyAsync(dants, ants, nin * sizeof(float2), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) {
     st = xcorr_run(ants_dev ? (const float2 *)ants : dants, nant, nfft, nchan, fftwidth, precision, engine, autos,
-                   out_dev ? (float2 *)accum : dout, chan, T, vsum, vcomp, s, &msg);
+                   out_dev ? (float2 *)accum : dout, chan, T, pairs, vsum, vcomp, s, &msg);
     if (st == GXC_OK && !out_dev)
       e = cudaMemcpyAsync(accum, dout, nvis * sizeof(float2), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -156,6 +158,7 @@ extern "C" gxc_status gxc_xcorr(const float *ants, int nant, int nfft, int nchan
     if (e == cudaSuccess && flag) st = GXC_ERR_TIMEOUT;
   }
   cudaFree(chan);
+  cudaFree(pairs);
   cudaFree(vsum);
   cudaFree(vcomp);
   cudaFree(dants);

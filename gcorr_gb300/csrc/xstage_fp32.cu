@@ -12,6 +12,8 @@
 // antenna-tile pairs; a thread owns one channel and one pair of 2-antenna tiles
 // (J <= K), i.e. a 2x2 block of antenna baselines x 4 products = 16 complex
 // accumulators, reused over TT FFTs staged in shared memory.
+#include <vector>
+
 #include "gxc_internal.h"
 
 namespace gxc {
@@ -116,67 +118,22 @@ __global__ void xstage_cc_kernel(const InT *__restrict__ chan, int nant, int nch
     }
 }
 
-// Tile-pair table (J <= K over ceil(nant/2) antenna tiles), cached per nant.
-static int2 *g_pairs = nullptr;
-static int g_pairs_nant = -1;
-static int g_pairs_dev = -1;
-
-static cudaError_t get_pairs(int nant, int2 **out, int *npairs) {
+// Tile-pair table J <= K over ceil(nant/2) antenna tiles, J-major, in device memory.
+cudaError_t make_tile_pairs(int nant, int2 **out) {
   const int nat = (nant + 1) / 2;
-  *npairs = nat * (nat + 1) / 2;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (g_pairs && g_pairs_nant == nant && g_pairs_dev == dev) {
-    *out = g_pairs;
-    return cudaSuccess;
-  }
-  int2 *h = new int2[*npairs];
+  const int npairs = nat * (nat + 1) / 2;
+  std::vector<int2> h((size_t)npairs);
   int q = 0;
   for (int J = 0; J < nat; J++)
-    for (int K = J; K < nat; K++) h[q++] = make_int2(J, K);
-  int2 *d = nullptr;
-  cudaError_t e = cudaMalloc(&d, sizeof(int2) * (size_t)(*npairs));
-  if (e == cudaSuccess) e = cudaMemcpy(d, h, sizeof(int2) * (size_t)(*npairs), cudaMemcpyHostToDevice);
-  delete[] h;
-  if (e != cudaSuccess) return e;
-  // the previous table stays allocated until process exit (another handle may use it)
-  g_pairs = d;
-  g_pairs_nant = nant;
-  g_pairs_dev = dev;
-  *out = d;
-  return cudaSuccess;
+    for (int K = J; K < nat; K++) h[(size_t)q++] = make_int2(J, K);
+  cudaError_t e = cudaMalloc((void **)out, sizeof(int2) * (size_t)npairs);
+  if (e == cudaSuccess) e = cudaMemcpy(*out, h.data(), sizeof(int2) * (size_t)npairs, cudaMemcpyHostToDevice);
+  return e;
 }
 
 cudaError_t launch_xstage_cuda_core(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,
-                                    float2 *vsum, float2 *vcomp, cudaStream_t s) {
-  if (nt <= 0) return cudaSuccess;
-  int2 *pairs = nullptr;
-  int npairs = 0;
-  cudaError_t e = get_pairs(nant, &pairs, &npairs);
-  if (e != cudaSuccess) return e;
-  const int nstream = 2 * nant;
-  const size_t esz = chan_type == CHAN_F32 ? sizeof(float2) : sizeof(__half2);
-  const int pairs_per_cta = npairs < 64 ? npairs : 64;
-  const int threads = pairs_per_cta * CW;
-  int TT = (int)(65536 / ((size_t)nstream * CW * esz));
-  if (TT < 1) TT = 1;
-  if (TT > 32) TT = 32;
-  const size_t smem = (size_t)TT * nstream * CW * esz;
-  dim3 grid((unsigned)((npairs + pairs_per_cta - 1) / pairs_per_cta), (unsigned)((nchan + CW - 1) / CW));
-  if (chan_type == CHAN_F32) {
-    auto k = xstage_cc_kernel<float2>;
-    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k<<<grid, threads, smem, s>>>((const float2 *)chan, nant, nchan, T, nt, autos, pairs, npairs, pairs_per_cta, TT,
-                                   vsum, vcomp);
-  } else {
-    auto k = xstage_cc_kernel<__half2>;
-    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k<<<grid, threads, smem, s>>>((const __half2 *)chan, nant, nchan, T, nt, autos, pairs, npairs, pairs_per_cta, TT,
-                                   vsum, vcomp);
-  }
-  return cudaGetLastError();
+                                    const int2 *pairs, float2 *vsum, float2 *vcomp, cudaStream_t s) {
+  return launch_xstage_cuda_core_pairs(chan, chan_type, nant, nchan, T, nt, autos, pairs, vsum, vcomp, s);
 }
 
 // Same launch with a caller-provided tile-pair table (J <= K over ceil(nant/2)

@@ -130,6 +130,30 @@ int gxc_fft_block(const gxc_handle *h);
 gxc_status gxc_enable_stage_timing(gxc_handle *h, int enable);
 gxc_status gxc_stage_times(gxc_handle *h, float *f_ms, float *x_ms, float *total_ms);
 
+/* Batches of independent jobs of uneven size (antenna counts, channel counts,
+ * formats, lengths), launched as one CUDA graph whose parallel branches are the
+ * jobs' launch sequences; the GPU overlaps the jobs.  The reference runs one
+ * FxKernel per sub-integration and thread (fxkernel/src/bench_fxkernel.cpp:93-139)
+ * and has no batch API; this replaces that thread replication on one GPU.
+ * inputs are device pointers (16-byte aligned); inputs and delays are fixed when
+ * the batch is created (create a new batch to change them).  Creation runs every
+ * job once.  Results: gxc_get_visibilities(gxc_batch_job(b, i), out) after the
+ * launch's stream has completed. */
+typedef struct gxc_job {
+  gxc_config cfg;
+  const uint8_t *const *inputs; /* [nant] device buffers */
+  const double *poly;           /* [nant][3] */
+  const double *fso;            /* [nant] */
+} gxc_job;
+typedef struct gxc_batch gxc_batch;
+gxc_status gxc_batch_create(const gxc_job *jobs, int njobs, gxc_batch **out);
+gxc_status gxc_batch_launch(gxc_batch *b, void *stream);
+int gxc_batch_size(const gxc_batch *b);
+gxc_handle *gxc_batch_job(gxc_batch *b, int i);
+/* Kernel launches one batch launch contains (the sum over its jobs). */
+int gxc_batch_launch_count(const gxc_batch *b);
+gxc_status gxc_batch_destroy(gxc_batch *b);
+
 /* The X-stage alone, on already-channelised data, as the reference GPU X kernels
  * take it (gcorr/src/gxkernel.h:86-88, CrossCorrAccumHoriz/CCAH2/CCAH3;
  * layout gcorr/src/gxkernel.h:30-44): ants is complex float

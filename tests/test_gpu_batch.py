@@ -1,0 +1,61 @@
+"""GPU tests of the batch API (uneven jobs in one graph launch) and the autotuner."""
+import numpy as np
+import pytest
+
+from gcorr_gb300 import FxKernel, synth
+from gcorr_gb300.batch import Batch
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+JOBS = [synth.Workload(nant=3, nchan=256, nfft=40, bw_hz=32e6, seed=1),
+        synth.Workload(nant=5, nchan=512, nfft=30, nbit=8, is_complex=True, bw_hz=32e6, seed=2),
+        synth.Workload(nant=4, nchan=1024, nfft=24, bw_hz=64e6, seed=3),
+        synth.Workload(nant=2, nchan=16384, nfft=4, bw_hz=64e6, seed=4)]
+
+
+def _job(w, d, **kw):
+    return dict(nant=w.nant, nchan=w.nchan, nfft=w.nfft, nbit=w.nbit, lo=w.lo_hz, bw=w.bw_hz,
+                is_complex=w.is_complex, inputs=d["inputs"], poly=d["poly"], fso=d["fso"], **kw)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_batch_matches_individual_runs(precision):
+    data = [synth.random_bytes(w, device="cuda") for w in JOBS]
+    b = Batch([_job(w, d, precision=precision) for w, d in zip(JOBS, data)])
+    b.launch()
+    b.launch()  # the graph replays from the same inputs
+    for i, (w, d) in enumerate(zip(JOBS, data)):
+        fx = FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=precision)
+        fx.setInputData(d["inputs"])
+        fx.setDelays(d["poly"], d["fso"])
+        fx.process()
+        ref = fx.visibilities()
+        assert np.array_equal(b.baseline_counts(i), fx.baseline_counts())
+        fx.close()
+        assert O.rel_rms(b.visibilities(i), ref) < 1e-6, i
+    assert b.launches > 0
+    b.close()
+
+
+def test_batch_vs_fp64_oracle():
+    data = [synth.random_bytes(w, device="cuda") for w in JOBS[:3]]
+    b = Batch([_job(w, d, precision="fp32") for w, d in zip(JOBS[:3], data)])
+    b.launch()
+    for i, (w, d) in enumerate(zip(JOBS[:3], data)):
+        inputs = [x.cpu().numpy() for x in d["inputs"]]
+        ref, rc = O.exact_process(O.config_from_workload(w, O.ROT_EXACT, True), inputs, d["poly"], d["fso"])
+        assert np.array_equal(b.baseline_counts(i), rc)
+        assert O.rel_rms_per_product(b.visibilities(i), ref).max() < 1e-5
+    b.close()
+
+
+def test_autotune_caches(tmp_path):
+    from gcorr_gb300.autotune import tune
+    w = JOBS[2]
+    d = synth.random_bytes(w, device="cuda")
+    path = str(tmp_path / "tune.json")
+    r1 = tune(_job(w, d, precision="fp16"), blocks=(8, 24), path=path)
+    assert r1["fft_block"] in (8, 24) and r1["x_engine"] in ("tensor", "cuda_core") and r1["tried"]
+    r2 = tune(_job(w, d, precision="fp16"), blocks=(8, 24), path=path)
+    assert r2 == r1
