@@ -411,6 +411,9 @@ def main():
     def step():
         fx.process(stream=sptr, sync=False)
 
+    # per-launch stage events stay on through the timed steps: the roofline below uses the
+    # last timed step's F and X launch durations, recorded on the launching stream
+    fx.enable_stage_timing(True)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -434,11 +437,10 @@ def main():
     ms_max = reduce_max(ms, world, dev)
     clocks = clk.summary()
 
-    # stage split (separate, untimed run with per-block events)
-    fx.enable_stage_timing(True)
-    step()
     f_ms, x_ms, tot_ms = fx.stage_times()
     fx.enable_stage_timing(False)
+    fft_block = fx.fft_block
+    nlaunch = -(-w.nfft // fft_block)
     vis0 = fx.visibilities()
 
     # X-stage comparison (untimed): the same sub-integration through each X engine
@@ -510,7 +512,8 @@ def main():
                "matches_device_run": bool(np.allclose(vis_h, vis0, rtol=1e-5, atol=1e-6))}
         fxh.close()
 
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel, per launch: algorithmic bytes of one launch (units = FFTs
+    # of all streams it processes) over that kernel's average launch duration in the timed step
     pk = peaks()
     esz = 8 if args.precision == "fp32" else 4
     in_bytes = w.bytes_per_antenna * w.nant
@@ -518,20 +521,34 @@ def main():
     nprod = 4 * w.nant * (w.nant + 1) // 2
     xflops = 8.0 * nprod * w.nchan * w.nfft
     fftflops = 5.0 * w.fft_len * np.log2(w.fft_len) * 2 * w.nant * w.nfft
-    f_gbs = (in_bytes + chan_bytes) / (f_ms / 1e3) / 1e9
-    x_gbs = chan_bytes / (x_ms / 1e3) / 1e9
-    if f_ms >= x_ms:
-        roof = {"kernel": "fstage_kernel (unpack+rotate+FFT+frac-delay)", "bound": "hbm", "achieved": f_gbs,
-                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": f_gbs / pk["hbm_gbs"], "traffic": None,
-                "algorithmic_bytes_per_step": in_bytes + chan_bytes, "fft_tflops": fftflops / (f_ms / 1e3) / 1e12,
-                "peak_source": pk["source"]}
-    else:
-        roof = {"kernel": "xstage", "bound": "hbm", "achieved": x_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": x_gbs / pk["hbm_gbs"], "traffic": None, "algorithmic_bytes_per_step": chan_bytes,
-                "x_tflops": xflops / (x_ms / 1e3) / 1e12, "peak_source": pk["source"]}
+    ffts_per_launch = w.nfft / nlaunch
+    f_launch_ms, x_launch_ms = f_ms / nlaunch, x_ms / nlaunch
+    f_bytes = (in_bytes + chan_bytes) / nlaunch
+    x_bytes = chan_bytes / nlaunch
+    fp32_peak = 152 * 128 * 2 * (clocks.get("sm_mhz") or 2070.0) * 1e6 / 1e12  # FP32 FMA lanes, nominal
+    tdata = {}
     tfile = os.path.join(ROOT, "profiles", f"traffic_{args.config}_{args.precision}.json")
     if os.path.exists(tfile):
-        roof["traffic"] = json.load(open(tfile)).get(roof["kernel"].split()[0])
+        tdata = json.load(open(tfile))
+
+    def traffic(key):
+        t = tdata.get(key)
+        return None if not t else t["per_fft"] * ffts_per_launch + t.get("per_launch_const", 0)
+
+    if f_ms >= x_ms:
+        roof = {"kernel": "fstage_kernel (unpack+rotate+FFT+frac-delay)", "bound": "hbm",
+                "achieved": f_bytes / (f_launch_ms / 1e3) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "traffic": traffic("fstage_kernel"), "algorithmic_bytes_per_launch": f_bytes,
+                "launch_ms": f_launch_ms, "launches_per_step": nlaunch, "ffts_per_launch": ffts_per_launch,
+                "fft_tflops": fftflops / (f_ms / 1e3) / 1e12, "fp32_peak_tflops_nominal": fp32_peak}
+        roof["fp32_pipe_frac_nominal"] = roof["fft_tflops"] / fp32_peak
+    else:
+        roof = {"kernel": "xstage", "bound": "hbm", "achieved": x_bytes / (x_launch_ms / 1e3) / 1e9,
+                "peak": pk["hbm_gbs"], "unit": "GB/s", "traffic": traffic("xstage"),
+                "algorithmic_bytes_per_launch": x_bytes, "launch_ms": x_launch_ms, "launches_per_step": nlaunch,
+                "ffts_per_launch": ffts_per_launch, "x_tflops": xflops / (x_ms / 1e3) / 1e12}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["peak_source"] = pk["source"] + " (MEASURED_PEAKS.json hbm_gbs)" if pk["source"] == "measured" else "fallback"
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
