@@ -27,7 +27,9 @@ EXPORTS = [
     "gxc_sync", "gxc_accumulate", "gxc_get_visibilities", "gxc_device_visibilities", "gxc_get_baseline_counts",
     "gxc_get_valid_flags", "gxc_last_error", "gxc_last_launch_count", "gxc_fft_block", "gxc_enable_stage_timing",
     "gxc_stage_times", "gxc_xcorr", "gxc_xcorr_noalloc", "gxc_batch_create", "gxc_batch_launch", "gxc_batch_size",
-    "gxc_batch_job", "gxc_batch_launch_count", "gxc_batch_destroy",
+    "gxc_batch_job", "gxc_batch_launch_count", "gxc_batch_destroy", "gxc_pipeline_create", "gxc_pipeline_submit",
+    "gxc_pipeline_wait", "gxc_pipeline_sync", "gxc_pipeline_integration", "gxc_pipeline_set_lin2circ",
+    "gxc_pipeline_handle", "gxc_pipeline_last_error", "gxc_pipeline_destroy", "gxc_lin2circ",
 ]
 
 
@@ -121,6 +123,26 @@ def lib():
         l.gxc_batch_launch_count.restype = C.c_int
         l.gxc_batch_destroy.argtypes = [V]
         l.gxc_batch_destroy.restype = C.c_int
+        l.gxc_pipeline_create.argtypes = [P(GxcConfig), C.c_int, C.c_int, P(V)]
+        l.gxc_pipeline_create.restype = C.c_int
+        l.gxc_pipeline_submit.argtypes = [V, V, V, V, V, P(C.c_int64)]
+        l.gxc_pipeline_submit.restype = C.c_int
+        l.gxc_pipeline_wait.argtypes = [V, C.c_int64]
+        l.gxc_pipeline_wait.restype = C.c_int
+        l.gxc_pipeline_sync.argtypes = [V]
+        l.gxc_pipeline_sync.restype = C.c_int
+        l.gxc_pipeline_integration.argtypes = [V, V, C.c_int, P(C.c_int)]
+        l.gxc_pipeline_integration.restype = C.c_int
+        l.gxc_pipeline_set_lin2circ.argtypes = [V, C.c_int, V]
+        l.gxc_pipeline_set_lin2circ.restype = C.c_int
+        l.gxc_pipeline_handle.argtypes = [V]
+        l.gxc_pipeline_handle.restype = V
+        l.gxc_pipeline_last_error.argtypes = [V]
+        l.gxc_pipeline_last_error.restype = C.c_char_p
+        l.gxc_pipeline_destroy.argtypes = [V]
+        l.gxc_pipeline_destroy.restype = C.c_int
+        l.gxc_lin2circ.argtypes = [V, V, C.c_int, C.c_int, C.c_int, V]
+        l.gxc_lin2circ.restype = C.c_int
         _lib = l
     return _lib
 

@@ -16,7 +16,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgxcorr.so")
-SOURCES = ["gxc_api.cu", "fstage.cu", "xstage_fp32.cu", "xstage_tc.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "batch_api.cu"]
+SOURCES = ["gxc_api.cu", "fstage.cu", "xstage_fp32.cu", "xstage_tc.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "batch_api.cu",
+           "pipeline_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -34,10 +34,6 @@ struct gxc_handle {
   uint8_t *d_inbuf = nullptr;          // staging for host inputs [nant][bytes_per_ant]
   const uint8_t **d_inptrs = nullptr;  // device array of per-antenna device pointers
   double *d_poly = nullptr, *d_fso = nullptr;
-  // pinned upload staging: [nant pointers][nant*3 poly][nant fso]
-  unsigned char *h_stage = nullptr;
-  size_t stage_bytes = 0;
-  cudaEvent_t ev_upload = nullptr;
   std::vector<double> poly, fso;
 
   // state
@@ -188,8 +184,6 @@ static void release(gxc_handle *h) {
   cudaFree(h->d_vsum);
   cudaFree(h->d_vcomp);
   cudaFree(h->d_vis);
-  if (h->h_stage) cudaFreeHost(h->h_stage);
-  if (h->ev_upload) cudaEventDestroy(h->ev_upload);
   if (h->ev_done) cudaEventDestroy(h->ev_done);
   for (cudaEvent_t e : h->ev_stage) cudaEventDestroy(e);
   if (h->ev_begin) cudaEventDestroy(h->ev_begin);
@@ -301,9 +295,6 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   A((void **)&h->d_vis, sizeof(float2) * nvis);
   if (e == cudaSuccess) e = make_twiddles(h->F, &h->d_tw);
   if (e == cudaSuccess) e = make_tile_pairs(nant, &h->d_pairs);
-  h->stage_bytes = sizeof(uint8_t *) * nant + sizeof(double) * 4 * nant;
-  if (e == cudaSuccess) e = cudaMallocHost((void **)&h->h_stage, h->stage_bytes);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_upload, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMemset(h->d_vis, 0, sizeof(float2) * nvis);
   if (e != cudaSuccess) {
@@ -394,6 +385,25 @@ __global__ void finalize_kernel(const float2 *__restrict__ vsum, const float2 *_
   vis[i] = make_float2(re, im);
 }
 
+// Per-call parameters of up to kAnt antennas (about 10 KB: kernel parameters of up to
+// 32 KB are allowed on this architecture).
+struct UploadChunk {
+  static constexpr int kAnt = 256;
+  int a0, n;
+  const uint8_t *ptrs[kAnt];
+  double poly[3 * kAnt];
+  double fso[kAnt];
+};
+
+__global__ void upload_kernel(const __grid_constant__ UploadChunk u, const uint8_t **d_ptrs, double *d_poly,
+                              double *d_fso) {
+  for (int i = threadIdx.x; i < u.n; i += blockDim.x) {
+    d_ptrs[u.a0 + i] = u.ptrs[i];
+    d_fso[u.a0 + i] = u.fso[i];
+    for (int j = 0; j < 3; j++) d_poly[3 * (u.a0 + i) + j] = u.poly[3 * i + j];
+  }
+}
+
 __global__ void add_kernel(float *__restrict__ dst, const float *__restrict__ src, size_t n) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] += src[i];
@@ -409,30 +419,30 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
   const int nant = c.nant;
   int launches = 0;
 
-  // upload pointers + delay model through pinned staging (wait for the previous upload;
-  // not while the stream is being captured into a graph, whose replays reuse the staging)
+  // input pointers and the delay model travel as kernel parameters of a one-block upload
+  // kernel (no host->device memcpy on the stream: small copies would queue on the copy
+  // engine behind bulk input copies of other streams, and need no host wait here)
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   GXC_CUDA(h, cudaStreamIsCapturing(s, &cap), "querying stream capture");
   const bool capturing = cap != cudaStreamCaptureStatusNone;
-  if (!capturing) GXC_CUDA(h, cudaEventSynchronize(h->ev_upload), "waiting for the previous upload");
   // inside a capture the handle's events become graph nodes that record on every replay,
   // so sync() and the getters wait for the latest graph launch; stage timing is off there
   const unsigned rec_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   const bool timing = h->stage_timing && !capturing;
-  const uint8_t **sp = (const uint8_t **)h->h_stage;
-  double *spoly = (double *)(h->h_stage + sizeof(uint8_t *) * nant);
-  double *sfso = spoly + 3 * nant;
-  for (int a = 0; a < nant; a++)
-    sp[a] = h->input_on_host ? h->d_inbuf + (size_t)a * h->bytes_per_ant : h->user_ptrs[a];
-  memcpy(spoly, h->poly.data(), sizeof(double) * 3 * nant);
-  memcpy(sfso, h->fso.data(), sizeof(double) * nant);
-  GXC_CUDA(h, cudaMemcpyAsync((void *)h->d_inptrs, sp, sizeof(uint8_t *) * nant, cudaMemcpyHostToDevice, s),
-           "uploading input pointers");
-  GXC_CUDA(h, cudaMemcpyAsync(h->d_poly, spoly, sizeof(double) * 3 * nant, cudaMemcpyHostToDevice, s),
-           "uploading delays");
-  GXC_CUDA(h, cudaMemcpyAsync(h->d_fso, sfso, sizeof(double) * nant, cudaMemcpyHostToDevice, s),
-           "uploading file start offsets");
-  GXC_CUDA(h, cudaEventRecordWithFlags(h->ev_upload, s, rec_flags), "recording the upload event");
+  for (int a0 = 0; a0 < nant; a0 += UploadChunk::kAnt) {
+    UploadChunk u;
+    u.a0 = a0;
+    u.n = nant - a0 < UploadChunk::kAnt ? nant - a0 : UploadChunk::kAnt;
+    for (int i = 0; i < u.n; i++) {
+      const int a = a0 + i;
+      u.ptrs[i] = h->input_on_host ? h->d_inbuf + (size_t)a * h->bytes_per_ant : h->user_ptrs[a];
+      for (int j = 0; j < 3; j++) u.poly[3 * i + j] = h->poly[3 * (size_t)a + j];
+      u.fso[i] = h->fso[a];
+    }
+    upload_kernel<<<1, 128, 0, s>>>(u, h->d_inptrs, h->d_poly, h->d_fso);
+    GXC_CUDA(h, cudaGetLastError(), "upload kernel");
+    launches++;
+  }
   if (h->input_on_host) {
     for (int a = 0; a < nant; a++)
       GXC_CUDA(h,

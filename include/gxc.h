@@ -154,6 +154,47 @@ gxc_handle *gxc_batch_job(gxc_batch *b, int i);
 int gxc_batch_launch_count(const gxc_batch *b);
 gxc_status gxc_batch_destroy(gxc_batch *b);
 
+/* Streaming ingest of consecutive sub-integrations (one configuration) from host
+ * memory.  Replaces the reference GPU driver's copy-then-wait-for-the-previous-
+ * stream loop (gcorr/src/testgpukernel.cu:462-486) and the CPU driver's
+ * process()+accumulate() per sub-integration (fxkernel/src/testfxkernel.cpp:81-108).
+ * The pipeline owns `nslots` (1..8) device input slots, a copy stream and a
+ * compute stream: submit() enqueues the host->device copy of sub-integration
+ * k into slot k % nslots (after that slot's previous sub-integration finished)
+ * and its correlation behind that copy, so copies overlap the previous
+ * sub-integration's F and X stages.  submit() returns once the work is
+ * enqueued; inputs[a] and vis_out must stay valid and untouched until
+ * gxc_pipeline_wait(seq) returns.  Use pinned host memory (cudaHostAlloc /
+ * cudaHostRegister) for inputs and vis_out: pageable buffers make the copies
+ * synchronous and remove the overlap.  vis_out (optional; host or device) receives
+ * this sub-integration's visibilities in GXC_LAYOUT_FXKERNEL.  With integrate != 0
+ * every sub-integration's (normalised) visibilities are also added into a
+ * device-side compensated FP32 sum: the reference's accumulate() over a long
+ * integration (fxkernel/src/fxkernel.cpp:414-423), read by
+ * gxc_pipeline_integration (synchronises; reset != 0 clears it).
+ *
+ * Linear->circular polarisation conversion, the voltage-domain transform of
+ * examples/chris/bench/gpubench.cu:145-160 (P1' = g1*P1 - g2*P2,
+ * P2' = g1*P1 + g2*P2 per antenna and channel), applied exactly to the
+ * visibilities as V' = J_j V J_k^H with J = [[g1, -g2], [g1, g2]].  gains:
+ * complex float [nant][2][nchan] (g1 then g2 per antenna), host or device; null =
+ * ideal feeds, g1 = 1/sqrt(2), g2 = i/sqrt(2).  gxc_pipeline_set_lin2circ applies it
+ * to every later sub-integration before integration and copy-out; gxc_lin2circ
+ * converts a device buffer [nbl][4][nchan] in place (gains then device memory or
+ * null) on `stream`. */
+typedef struct gxc_pipeline gxc_pipeline;
+gxc_status gxc_pipeline_create(const gxc_config *cfg, int nslots, int integrate, gxc_pipeline **out);
+gxc_status gxc_pipeline_submit(gxc_pipeline *p, const uint8_t *const *inputs, const double *poly, const double *fso,
+                               float *vis_out, int64_t *seq);
+gxc_status gxc_pipeline_wait(gxc_pipeline *p, int64_t seq);
+gxc_status gxc_pipeline_sync(gxc_pipeline *p);
+gxc_status gxc_pipeline_integration(gxc_pipeline *p, float *out, int reset, int *nsub);
+gxc_status gxc_pipeline_set_lin2circ(gxc_pipeline *p, int enable, const float *gains);
+gxc_handle *gxc_pipeline_handle(gxc_pipeline *p);
+const char *gxc_pipeline_last_error(const gxc_pipeline *p);
+gxc_status gxc_pipeline_destroy(gxc_pipeline *p);
+gxc_status gxc_lin2circ(float *vis, const float *gains, int nant, int nchan, int autos, void *stream);
+
 /* The X-stage alone, on already-channelised data, as the reference GPU X kernels
  * take it (gcorr/src/gxkernel.h:86-88, CrossCorrAccumHoriz/CCAH2/CCAH3;
  * layout gcorr/src/gxkernel.h:30-44): ants is complex float

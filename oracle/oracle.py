@@ -223,3 +223,40 @@ def rel_rms_per_product(a, b):
     num = np.sqrt(np.sum(np.abs(a - b) ** 2, axis=-1))
     den = np.sqrt(np.sum(np.abs(b) ** 2, axis=-1))
     return num / np.where(den > 0, den, 1.0)
+
+
+# ---------------------------------------------------------------- polarisation conversion (test oracle)
+def lin2circ_voltages(x, gains=None):
+    """Voltage-domain linear->circular conversion of channelised data x[nant][2][..][nchan]
+    (complex), restating examples/chris/bench/gpubench.cu:145-160: per antenna and
+    channel, P1' = g1*P1 - g2*P2, P2' = g1*P1 + g2*P2.  gains [nant][2][nchan]
+    (g1, g2); None = ideal feeds g1 = 1/sqrt2, g2 = i/sqrt2."""
+    x = np.asarray(x, dtype=np.complex128)
+    nant, nchan = x.shape[0], x.shape[-1]
+    if gains is None:
+        g = np.empty((nant, 2, nchan), np.complex128)
+        g[:, 0] = 1 / np.sqrt(2)
+        g[:, 1] = 1j / np.sqrt(2)
+    else:
+        g = np.asarray(gains, dtype=np.complex128).reshape(nant, 2, nchan)
+    shape = (nant,) + (1,) * (x.ndim - 3) + (nchan,)
+    p1 = x[:, 0] * g[:, 0].reshape(shape)
+    p2 = x[:, 1] * g[:, 1].reshape(shape)
+    return np.stack([p1 - p2, p1 + p2], axis=1)
+
+
+def correlate_voltages(x, autos=True):
+    """Visibilities [nbl][4][nchan] of channelised voltages x[nant][2][nfft][nchan]:
+    mean over FFTs of X_j,l * conj(X_k,m), crosses in fxkernel order
+    (fxkernel/src/fxkernel.cpp:328-355) then autos."""
+    x = np.asarray(x, dtype=np.complex128)
+    nant = x.shape[0]
+    pairs = [(j, k) for j in range(nant - 1) for k in range(j + 1, nant)]
+    if autos:
+        pairs += [(j, j) for j in range(nant)]
+    out = np.empty((len(pairs), 4, x.shape[-1]), np.complex128)
+    for b, (j, k) in enumerate(pairs):
+        for l in range(2):
+            for m in range(2):
+                out[b, 2 * l + m] = (x[j, l] * np.conj(x[k, m])).mean(axis=0)
+    return out
