@@ -14,11 +14,12 @@ GXC_ERR_CUDA = 3
 GXC_ERR_OUT_OF_MEMORY = 4
 GXC_ERR_STATE = 5
 GXC_ERR_TIMEOUT = 6
+GXC_END_OF_DATA = 7
 GXC_PRECISION_FP32, GXC_PRECISION_FP16, GXC_PRECISION_FP8 = 0, 1, 2
 GXC_ROTATOR_EXACT, GXC_ROTATOR_FXKERNEL = 0, 1
 GXC_XENGINE_AUTO, GXC_XENGINE_CUDA_CORE, GXC_XENGINE_TENSOR = 0, 1, 2
 _STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "out of memory",
-           5: "bad call order", 6: "device wait timed out"}
+           5: "bad call order", 6: "device wait timed out", 7: "end of data"}
 
 # every function include/gxc.h declares (the CPU tests check the export list against the header)
 EXPORTS = [
@@ -30,6 +31,10 @@ EXPORTS = [
     "gxc_batch_job", "gxc_batch_launch_count", "gxc_batch_destroy", "gxc_pipeline_create", "gxc_pipeline_submit",
     "gxc_pipeline_wait", "gxc_pipeline_sync", "gxc_pipeline_integration", "gxc_pipeline_set_lin2circ",
     "gxc_pipeline_handle", "gxc_pipeline_last_error", "gxc_pipeline_destroy", "gxc_lin2circ",
+    "gxc_conf_read", "gxc_conf_config", "gxc_conf_int", "gxc_conf_double", "gxc_conf_antenna_name",
+    "gxc_conf_antenna_file", "gxc_conf_delays", "gxc_conf_free", "gxc_reader_open", "gxc_reader_read",
+    "gxc_reader_close", "gxc_save_visibilities", "gxc_host_alloc", "gxc_host_free", "gxc_set_frame_validity",
+    "gxc_vdif_parse_header", "gxc_vdif_depacketize",
 ]
 
 
@@ -38,6 +43,13 @@ class GxcConfig(C.Structure):
                 ("is_complex", C.c_int), ("lo_hz", C.c_double), ("bw_hz", C.c_double), ("precision", C.c_int),
                 ("rotator", C.c_int), ("autos", C.c_int), ("x_engine", C.c_int), ("fft_block", C.c_int),
                 ("device", C.c_int)]
+
+
+class GxcVdifHeader(C.Structure):
+    _fields_ = [("invalid", C.c_int), ("legacy", C.c_int), ("seconds", C.c_int64), ("ref_epoch", C.c_int),
+                ("frame", C.c_int), ("version", C.c_int), ("nchan", C.c_int), ("frame_bytes", C.c_int),
+                ("is_complex", C.c_int), ("bits", C.c_int), ("thread", C.c_int), ("station", C.c_int),
+                ("header_bytes", C.c_int)]
 
 
 class GxcJob(C.Structure):
@@ -143,6 +155,41 @@ def lib():
         l.gxc_pipeline_destroy.restype = C.c_int
         l.gxc_lin2circ.argtypes = [V, V, C.c_int, C.c_int, C.c_int, V]
         l.gxc_lin2circ.restype = C.c_int
+        l.gxc_conf_read.argtypes = [C.c_char_p, P(V)]
+        l.gxc_conf_read.restype = C.c_int
+        l.gxc_conf_config.argtypes = [V, P(GxcConfig)]
+        l.gxc_conf_config.restype = C.c_int
+        l.gxc_conf_int.argtypes = [V, C.c_char_p]
+        l.gxc_conf_int.restype = C.c_int
+        l.gxc_conf_double.argtypes = [V, C.c_char_p]
+        l.gxc_conf_double.restype = C.c_double
+        l.gxc_conf_antenna_name.argtypes = [V, C.c_int]
+        l.gxc_conf_antenna_name.restype = C.c_char_p
+        l.gxc_conf_antenna_file.argtypes = [V, C.c_int]
+        l.gxc_conf_antenna_file.restype = C.c_char_p
+        l.gxc_conf_delays.argtypes = [V, V, V]
+        l.gxc_conf_delays.restype = C.c_int
+        l.gxc_conf_free.argtypes = [V]
+        l.gxc_conf_free.restype = None
+        l.gxc_reader_open.argtypes = [V, C.c_int, C.c_size_t, P(V)]
+        l.gxc_reader_open.restype = C.c_int
+        l.gxc_reader_read.argtypes = [V, V]
+        l.gxc_reader_read.restype = C.c_int
+        l.gxc_reader_close.argtypes = [V]
+        l.gxc_reader_close.restype = C.c_int
+        l.gxc_save_visibilities.argtypes = [C.c_char_p, V, C.c_int, C.c_int, C.c_double]
+        l.gxc_save_visibilities.restype = C.c_int
+        l.gxc_host_alloc.argtypes = [C.c_size_t, P(V)]
+        l.gxc_host_alloc.restype = C.c_int
+        l.gxc_host_free.argtypes = [V]
+        l.gxc_host_free.restype = C.c_int
+        l.gxc_set_frame_validity.argtypes = [V, V, C.c_size_t, C.c_int64]
+        l.gxc_set_frame_validity.restype = C.c_int
+        l.gxc_vdif_parse_header.argtypes = [V, P(GxcVdifHeader)]
+        l.gxc_vdif_parse_header.restype = C.c_int
+        l.gxc_vdif_depacketize.argtypes = [V, C.c_size_t, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, C.c_int,
+                                           C.c_int, C.c_uint8, V, C.c_size_t, V, V, V]
+        l.gxc_vdif_depacketize.restype = C.c_int
         _lib = l
     return _lib
 

@@ -17,8 +17,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgxcorr.so")
 SOURCES = ["gxc_api.cu", "fstage.cu", "xstage_fp32.cu", "xstage_tc.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "batch_api.cu",
-           "pipeline_api.cu"]
+           "pipeline_api.cu", "conf_io.cpp", "vdif.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# command-line drivers with the reference harness's interface, linked against the library
+APPS = ["testfxkernel", "bench_fxkernel"]
+BIN = os.path.join(HERE, "bin")
 
 
 def nvcc() -> str:
@@ -48,7 +51,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     objs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _needs(o, [s] + headers):
             jobs.append([nvcc(), "-c", s, "-o", o] + flags() + (["-Xptxas", "-v"] if verbose else []))
@@ -70,7 +73,28 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if r.returncode:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
+    build_apps(force=force)
     return LIB
+
+
+def build_apps(force: bool = False) -> None:
+    os.makedirs(BIN, exist_ok=True)
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("no C++ compiler for the command-line drivers")
+    hdrs = [os.path.join(ROOT, "include", h) for h in ("gxc.h", "fxkernel_gxc.h", "gxc_common.h")]
+    jobs = []
+    for app in APPS:
+        src = os.path.join(HERE, "apps", app + ".cpp")
+        exe = os.path.join(BIN, app)
+        if force or _needs(exe, [src, LIB] + hdrs):
+            jobs.append([cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", exe, "-L", HERE,
+                         "-lgxcorr", "-Wl,-rpath,$ORIGIN/..", "-pthread"])
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        for r, cmd in zip(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs), jobs):
+            if r.returncode:
+                sys.stderr.write(r.stdout + r.stderr)
+                raise RuntimeError("driver build failed: " + " ".join(cmd))
 
 
 if __name__ == "__main__":

@@ -50,6 +50,12 @@ __global__ void geometry_kernel(Job job) {
     if (off >= 0 && off <= job.maxoffset) {
       g.offset = (int)off;
       g.valid = 1;
+      const uint8_t *fv = job.fvalid ? job.fvalid[ant] : nullptr;
+      if (fv) {
+        const long long f1 = (off + job.F - 1) / job.samples_per_frame;
+        for (long long f = off / job.samples_per_frame; f <= f1; f++)
+          if (!fv[f]) g.valid = 0;
+      }
     }
   }
   job.geom[idx] = g;

@@ -34,6 +34,9 @@ struct gxc_handle {
   uint8_t *d_inbuf = nullptr;          // staging for host inputs [nant][bytes_per_ant]
   const uint8_t **d_inptrs = nullptr;  // device array of per-antenna device pointers
   double *d_poly = nullptr, *d_fso = nullptr;
+  // frame validity (gxc_set_frame_validity): user device pointers, uploaded per process()
+  std::vector<const uint8_t *> user_fvalid;
+  const uint8_t **d_fvalid = nullptr;
   std::vector<double> poly, fso;
 
   // state
@@ -161,6 +164,7 @@ const char *gxc_status_string(gxc_status s) {
     case GXC_ERR_OUT_OF_MEMORY: return "out of memory";
     case GXC_ERR_STATE: return "bad call order";
     case GXC_ERR_TIMEOUT: return "device wait timed out";
+    case GXC_END_OF_DATA: return "end of data";
   }
   return "unknown status";
 }
@@ -175,6 +179,7 @@ static void release(gxc_handle *h) {
   cudaFree((void *)h->d_inptrs);
   cudaFree(h->d_poly);
   cudaFree(h->d_fso);
+  cudaFree((void *)h->d_fvalid);
   cudaFree(h->d_geom);
   cudaFree(h->d_counts);
   cudaFree(h->d_valid);
@@ -277,6 +282,8 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   j.bw_hz = cfg->bw_hz;
   j.Ts = cfg->is_complex ? 1.0 / cfg->bw_hz : 1.0 / (2.0 * cfg->bw_hz);
   j.maxoffset = (long long)(cfg->nfft - 1) * h->F;
+  j.fvalid = nullptr;
+  j.samples_per_frame = 0;
 
   cudaError_t e = cudaSuccess;
   auto A = [&](void **p, size_t n) {
@@ -285,6 +292,7 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   A((void **)&h->d_inptrs, sizeof(uint8_t *) * nant);
   A((void **)&h->d_poly, sizeof(double) * 3 * nant);
   A((void **)&h->d_fso, sizeof(double) * nant);
+  A((void **)&h->d_fvalid, sizeof(uint8_t *) * nant);
   A((void **)&h->d_geom, sizeof(Geom) * (size_t)nant * cfg->nfft);
   A((void **)&h->d_counts, sizeof(int32_t) * (h->nbl > 0 ? h->nbl : 1));
   A((void **)&h->d_valid, (size_t)nant * cfg->nfft);
@@ -359,6 +367,37 @@ gxc_status gxc_set_input(gxc_handle *h, const uint8_t *const *per_ant, size_t by
   return GXC_OK;
 }
 
+gxc_status gxc_set_frame_validity(gxc_handle *h, const uint8_t *const *valid, size_t nframes,
+                                  int64_t samples_per_frame) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!valid) {
+    h->user_fvalid.clear();
+    h->job.fvalid = nullptr;
+    h->job.samples_per_frame = 0;
+    return GXC_OK;
+  }
+  if (samples_per_frame < 1) return fail(h, GXC_ERR_INVALID_ARGUMENT, "samples_per_frame must be >= 1");
+  const long long need = (long long)(h->cfg.nfft + 1) * h->F;  // every sample of the input buffer
+  if ((long long)nframes * samples_per_frame < need)
+    return fail(h, GXC_ERR_INVALID_ARGUMENT,
+                "frame validity covers " + std::to_string((long long)nframes * samples_per_frame) + " samples, need " +
+                    std::to_string(need));
+  cudaSetDevice(h->device);
+  for (int a = 0; a < h->cfg.nant; a++) {
+    if (!valid[a]) continue;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, valid[a]) != cudaSuccess ||
+        (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)) {
+      cudaGetLastError();
+      return fail(h, GXC_ERR_INVALID_ARGUMENT, "frame validity must be device memory");
+    }
+  }
+  h->user_fvalid.assign(valid, valid + h->cfg.nant);
+  h->job.fvalid = h->d_fvalid;
+  h->job.samples_per_frame = samples_per_frame;
+  return GXC_OK;
+}
+
 gxc_status gxc_set_delays(gxc_handle *h, const double *poly, const double *fso) {
   if (!h) return GXC_ERR_INVALID_ARGUMENT;
   if (!poly || !fso) return fail(h, GXC_ERR_INVALID_ARGUMENT, "null delay arrays");
@@ -391,14 +430,16 @@ struct UploadChunk {
   static constexpr int kAnt = 256;
   int a0, n;
   const uint8_t *ptrs[kAnt];
+  const uint8_t *fvalid[kAnt];
   double poly[3 * kAnt];
   double fso[kAnt];
 };
 
 __global__ void upload_kernel(const __grid_constant__ UploadChunk u, const uint8_t **d_ptrs, double *d_poly,
-                              double *d_fso) {
+                              double *d_fso, const uint8_t **d_fvalid) {
   for (int i = threadIdx.x; i < u.n; i += blockDim.x) {
     d_ptrs[u.a0 + i] = u.ptrs[i];
+    d_fvalid[u.a0 + i] = u.fvalid[i];
     d_fso[u.a0 + i] = u.fso[i];
     for (int j = 0; j < 3; j++) d_poly[3 * (u.a0 + i) + j] = u.poly[3 * i + j];
   }
@@ -438,8 +479,9 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
       u.ptrs[i] = h->input_on_host ? h->d_inbuf + (size_t)a * h->bytes_per_ant : h->user_ptrs[a];
       for (int j = 0; j < 3; j++) u.poly[3 * i + j] = h->poly[3 * (size_t)a + j];
       u.fso[i] = h->fso[a];
+      u.fvalid[i] = h->user_fvalid.empty() ? nullptr : h->user_fvalid[a];
     }
-    upload_kernel<<<1, 128, 0, s>>>(u, h->d_inptrs, h->d_poly, h->d_fso);
+    upload_kernel<<<1, 128, 0, s>>>(u, h->d_inptrs, h->d_poly, h->d_fso, h->d_fvalid);
     GXC_CUDA(h, cudaGetLastError(), "upload kernel");
     launches++;
   }

@@ -38,6 +38,11 @@ struct Job {
   int fractional_lo;             // fxkernel.cpp:67-71
   double lo_hz, bw_hz, Ts;
   long long maxoffset;           // (nfft-1)*F
+  // optional per-antenna frame validity (e.g. from a VDIF depacketiser): device array of nant
+  // pointers to uint8 [nframes] (a null entry = all valid); an FFT whose window touches an
+  // invalid frame is flagged.  fvalid == nullptr: no frame flags.
+  const uint8_t *const *fvalid;
+  long long samples_per_frame;
 };
 
 // Channelised-data element types.

@@ -112,6 +112,18 @@ class FxKernel:
         fso = np.ascontiguousarray(np.asarray(filestartoffsets, dtype=np.float64).reshape(self.nant))
         L.check(L.lib().gxc_set_delays(self._h, poly.ctypes.data, fso.ctypes.data), self._h, "setDelays")
 
+    def setFrameValidity(self, valid, samples_per_frame: int = 0):
+        """Per-antenna frame flags (device uint8 tensors, e.g. from vdif.depacketize), or None to clear."""
+        if valid is None:
+            L.check(L.lib().gxc_set_frame_validity(self._h, None, 0, 0), self._h, "setFrameValidity")
+            self._fvalid = None
+            return
+        ptrs = (C.c_void_p * self.nant)(*[_ptr(v) if v is not None else None for v in valid])
+        nframes = min(int(v.numel()) for v in valid if v is not None)
+        L.check(L.lib().gxc_set_frame_validity(self._h, C.cast(ptrs, C.c_void_p), nframes, int(samples_per_frame)),
+                self._h, "setFrameValidity")
+        self._fvalid = list(valid)
+
     def process(self, stream: Optional[int] = None, sync: bool = True):
         """One sub-integration; ``stream`` is a cudaStream_t address (torch: stream.cuda_stream)."""
         L.check(L.lib().gxc_process(self._h, C.c_void_p(stream or 0)), self._h, "process")

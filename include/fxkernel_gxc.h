@@ -112,21 +112,9 @@ class FxKernel {
 
   /* fxkernel/src/fxkernel.h:64 — text dump in the format of fxkernel.cpp:370-412 */
   void saveVisibilities(const char *outfile) {
-    std::ofstream f(outfile);
-    for (int c = 0; c < numchannels; c++) {
-      f << std::setw(5) << c << " " << std::setw(11) << std::fixed << std::setprecision(6)
-        << (c + 0.5) / numchannels * bandwidth / 1e6;
-      f << std::setprecision(5);
-      for (int b = 0; b < nbaselines; b++)
-        for (int p = 0; p < 4; p++) {
-          const cf32 v = vis[((size_t)b * 4 + p) * numchannels + c];
-          const float amp = std::sqrt(v.re * v.re + v.im * v.im);
-          const float ph = std::atan2(v.im, v.re);
-          f << " " << std::setw(11) << v.re << " " << std::setw(11) << v.im;
-          f << " " << std::setw(11) << amp << " " << std::setw(10) << ph;
-        }
-      f << std::endl;
-    }
+    check(gxc_save_visibilities(outfile, reinterpret_cast<const float *>(vis.data()), nbaselines, numchannels,
+                                bandwidth),
+          "saveVisibilities");
   }
 
   int baselines() const { return nbaselines; }

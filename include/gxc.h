@@ -41,7 +41,8 @@ typedef enum gxc_status {
   GXC_ERR_CUDA = 3,             /* a CUDA runtime call failed; see gxc_last_error */
   GXC_ERR_OUT_OF_MEMORY = 4,
   GXC_ERR_STATE = 5,            /* call order: process() before set_input()/set_delays() */
-  GXC_ERR_TIMEOUT = 6           /* a bounded device-side wait gave up */
+  GXC_ERR_TIMEOUT = 6,          /* a bounded device-side wait gave up */
+  GXC_END_OF_DATA = 7           /* a raw-file reader reached the end of a file (fxkernel/src/common.cpp:43-44) */
 } gxc_status;
 
 enum { GXC_PRECISION_FP32 = 0, GXC_PRECISION_FP16 = 1, GXC_PRECISION_FP8 = 2 };
@@ -98,6 +99,16 @@ gxc_status gxc_set_input(gxc_handle *h, const uint8_t *const *per_ant, size_t by
 /* FxKernel::setDelays (fxkernel/src/fxkernel.cpp:247-251): poly [nant][3], fso [nant]
  * (host memory).  Values are copied at this call. */
 gxc_status gxc_set_delays(gxc_handle *h, const double *poly, const double *fso);
+/* Optional per-antenna frame validity, e.g. from gxc_vdif_depacketize: valid[a]
+ * points at uint8 [nframes] device flags of antenna a's input (frame f holds
+ * samples [f*samples_per_frame, (f+1)*samples_per_frame) of the buffer; a null
+ * entry means all valid).  Every FFT whose window touches a zero flag is flagged
+ * like a window outside the buffer (not correlated, not counted).  nframes must
+ * cover the (nfft+1)*F samples of the buffer.  valid == NULL removes the flags.
+ * The reference has no such input: its data windows are only flagged by the
+ * delay geometry (fxkernel/src/fxkernel.cpp:288-309). */
+gxc_status gxc_set_frame_validity(gxc_handle *h, const uint8_t *const *valid, size_t nframes,
+                                  int64_t samples_per_frame);
 /* FxKernel::process (fxkernel/src/fxkernel.cpp:253-368): one sub-integration,
  * enqueued asynchronously on `stream` (a cudaStream_t; NULL = default stream).
  * Overwrites the handle's visibilities. */
@@ -194,6 +205,68 @@ gxc_handle *gxc_pipeline_handle(gxc_pipeline *p);
 const char *gxc_pipeline_last_error(const gxc_pipeline *p);
 gxc_status gxc_pipeline_destroy(gxc_pipeline *p);
 gxc_status gxc_lin2circ(float *vis, const float *gains, int nant, int nchan, int autos, void *stream);
+
+/* Harness file formats (host side).
+ * .conf files (fxkernel/src/common.cpp:54-114, parseConfig): keywords NBIT, NPOL,
+ * COMPLEX, NCHAN, LO, BANDWIDTH, NUMFFTS, NANT (case-insensitive), then NANT lines
+ * "name file p0 p1 p2 fso".  gxc_conf_config copies nant, nchan, nfft, nbit,
+ * is_complex, lo and bw into cfg and leaves its other fields alone; it returns
+ * GXC_ERR_UNSUPPORTED unless NPOL is 2.  gxc_conf_int takes NBIT, NPOL, COMPLEX,
+ * NCHAN, NUMFFTS or NANT (-1 otherwise); gxc_conf_double takes LO or BANDWIDTH.
+ * gxc_conf_delays fills poly[nant][3] and fso[nant] (either may be null).
+ * Raw files (common.cpp:38-52, readdata): each gxc_reader_read fills bufs[a] with
+ * the next bytes_per_read bytes of file a (files read in parallel) and returns
+ * GXC_END_OF_DATA when any file ends.
+ * gxc_save_visibilities writes vis ([nbl][4][nchan] complex float, host) in the
+ * vis.out text format of FxKernel::saveVisibilities (fxkernel/src/fxkernel.cpp:370-412).
+ * gxc_host_alloc / gxc_host_free: pinned host buffers, as allocDataHost uses for
+ * GPU input (common.cpp:3-36). */
+typedef struct gxc_conffile gxc_conffile;
+gxc_status gxc_conf_read(const char *path, gxc_conffile **out);
+gxc_status gxc_conf_config(const gxc_conffile *cf, gxc_config *cfg);
+int gxc_conf_int(const gxc_conffile *cf, const char *key);
+double gxc_conf_double(const gxc_conffile *cf, const char *key);
+const char *gxc_conf_antenna_name(const gxc_conffile *cf, int a);
+const char *gxc_conf_antenna_file(const gxc_conffile *cf, int a);
+gxc_status gxc_conf_delays(const gxc_conffile *cf, double *poly, double *fso);
+void gxc_conf_free(gxc_conffile *cf);
+typedef struct gxc_reader gxc_reader;
+gxc_status gxc_reader_open(const char *const *paths, int nant, size_t bytes_per_read, gxc_reader **out);
+gxc_status gxc_reader_read(gxc_reader *r, uint8_t *const *bufs);
+gxc_status gxc_reader_close(gxc_reader *r);
+gxc_status gxc_save_visibilities(const char *path, const float *vis, int nbl, int nchan, double bw_hz);
+gxc_status gxc_host_alloc(size_t bytes, void **out);
+gxc_status gxc_host_free(void *p);
+
+/* VDIF input.  gxc_vdif_parse_header decodes a 16- or 32-byte VDIF frame header
+ * (host memory; the fields the reference reads in examples/mark/dump_vdif.py:40-55).
+ * gxc_vdif_depacketize places the frames of one antenna's stream (device memory,
+ * nbytes of back-to-back frames of frame_bytes each, header included) into that
+ * antenna's engine input buffer `out` (device, nslots*payload_bytes bytes): the
+ * frame of second `s` and number `f` goes to slot (s - seconds0)*frames_per_second
+ * + f - frame0, as the reference's ingest orders frames (ingest/src/ingest.c:267-330).
+ * Frames that are marked invalid, malformed (length field != frame_bytes, payload !=
+ * payload_bytes), of another thread (thread_id >= 0) or outside [0, nslots) are
+ * skipped; valid[slot] (device, uint8 [nslots]) is 1 for a slot that was filled,
+ * and empty slots are set to `fill`.  Two-channel VDIF payloads are the engine's
+ * input layout (2-bit: channel = polarisation, codes 0..3 = the fxkernel levels;
+ * 8-bit complex: ch0 re, im, ch1 re, im); offset_binary_8bit != 0 converts 8-bit
+ * offset-binary samples to int8.  stats (device, optional) accumulates
+ * [accepted, skipped outside window / other thread, invalid or malformed].  Pass
+ * valid to gxc_set_frame_validity to flag the FFTs that touch empty slots.
+ * Asynchronous on `stream`. */
+typedef struct gxc_vdif_header {
+  int invalid, legacy;
+  int64_t seconds;   /* seconds from the reference epoch */
+  int ref_epoch;     /* half-years since 2000 */
+  int frame;         /* frame number within the second */
+  int version, nchan, frame_bytes, is_complex, bits, thread, station, header_bytes;
+} gxc_vdif_header;
+gxc_status gxc_vdif_parse_header(const uint8_t *header, gxc_vdif_header *out);
+gxc_status gxc_vdif_depacketize(const uint8_t *frames, size_t nbytes, int frame_bytes, int payload_bytes,
+                                int64_t seconds0, int frame0, int frames_per_second, int thread_id,
+                                int offset_binary_8bit, uint8_t fill, uint8_t *out, size_t nslots, uint8_t *valid,
+                                unsigned long long *stats, void *stream);
 
 /* The X-stage alone, on already-channelised data, as the reference GPU X kernels
  * take it (gcorr/src/gxkernel.h:86-88, CrossCorrAccumHoriz/CCAH2/CCAH3;

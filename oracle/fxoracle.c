@@ -604,6 +604,11 @@ int fxo_exact_channelise(const fxo_config *c, const uint8_t *input, const double
 
 int fxo_exact_process(const fxo_config *c, const uint8_t *const *inputs, const double *poly, const double *fso,
                       double *vis, int32_t *counts) {
+  return fxo_exact_process_masked(c, inputs, poly, fso, NULL, vis, counts);
+}
+
+int fxo_exact_process_masked(const fxo_config *c, const uint8_t *const *inputs, const double *poly,
+                             const double *fso, const uint8_t *mask, double *vis, int32_t *counts) {
   if (check_config(c)) return 1;
   const int na = c->nant, nc = c->nchan, F = fxo_fft_length(c);
   const int ncross = na * (na - 1) / 2, nbl = fxo_num_baselines(c);
@@ -617,6 +622,7 @@ int fxo_exact_process(const fxo_config *c, const uint8_t *const *inputs, const d
     for (int j = 0; j < na; j++) {
       double *x = X + (size_t)j * 4 * F;
       valid[j] = exact_station(c, inputs[j], poly + 3 * j, fso[j], i, x, x + F, x + 2 * F, x + 3 * F, tmp, tmp + 2 * F);
+      if (mask && !mask[(size_t)j * c->nfft + i]) valid[j] = 0;
     }
     for (int j = 0; j < na; j++) {
       if (!valid[j]) continue;

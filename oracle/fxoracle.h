@@ -71,6 +71,10 @@ int fxo_port_process_range(const fxo_config *c, const uint8_t *const *inputs, co
                            float *vis, int32_t *counts);
 int fxo_exact_process(const fxo_config *c, const uint8_t *const *inputs, const double *poly,
                       const double *fso, double *vis /* complex128 */, int32_t *counts);
+/* fxo_exact_process with extra per-(antenna, FFT) flags: mask [nant][nfft], 0 flags the
+ * FFT of that antenna on top of the geometry (NULL = no extra flags). */
+int fxo_exact_process_masked(const fxo_config *c, const uint8_t *const *inputs, const double *poly,
+                             const double *fso, const uint8_t *mask, double *vis, int32_t *counts);
 
 /* Channelised spectrum of one (antenna, FFT) after fringe rotation, FFT and
  * fractional-delay correction (before conjugation): 2 pols x nchan complex. */

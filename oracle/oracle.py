@@ -64,6 +64,8 @@ def lib():
         L.fxo_port_process_range.argtypes = [P(FxoConfig), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                              C.c_int, C.c_void_p, C.c_void_p]
         L.fxo_exact_process.argtypes = [P(FxoConfig), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.fxo_exact_process_masked.argtypes = [P(FxoConfig), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_void_p]
         L.fxo_port_channelise.argtypes = [P(FxoConfig), C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p]
         L.fxo_exact_channelise.argtypes = [P(FxoConfig), C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p]
         L.fxo_bytes_per_antenna.argtypes = [P(FxoConfig)]
@@ -140,15 +142,17 @@ def port_process_range(cfg: FxoConfig, inputs, poly, fso, fft_begin: int, fft_en
     return vis, counts
 
 
-def exact_process(cfg: FxoConfig, inputs, poly, fso):
-    """FP64 oracle; returns (vis complex128 [nbl,4,nchan], counts int32 [nbl])."""
+def exact_process(cfg: FxoConfig, inputs, poly, fso, mask=None):
+    """FP64 oracle; returns (vis complex128 [nbl,4,nchan], counts int32 [nbl]).
+    mask: optional uint8 [nant, nfft], 0 flags that antenna's FFT on top of the geometry."""
     arrs, ptrs = _inputs_array(inputs)
     poly, fso = _f64(poly), _f64(fso)
     nbl = nbaselines(cfg)
     vis = np.zeros((nbl, 4, cfg.nchan), dtype=np.complex128)
     counts = np.zeros(nbl, dtype=np.int32)
-    rc = lib().fxo_exact_process(C.byref(cfg), ptrs, poly.ctypes.data, fso.ctypes.data, vis.ctypes.data,
-                                 counts.ctypes.data)
+    m = None if mask is None else np.ascontiguousarray(np.asarray(mask, dtype=np.uint8).reshape(cfg.nant, cfg.nfft))
+    rc = lib().fxo_exact_process_masked(C.byref(cfg), ptrs, poly.ctypes.data, fso.ctypes.data,
+                                        None if m is None else m.ctypes.data, vis.ctypes.data, counts.ctypes.data)
     if rc:
         raise ValueError(f"fxo_exact_process failed ({rc})")
     return vis, counts
