@@ -146,13 +146,16 @@ gxc_status gxc_stage_times(gxc_handle *h, float *f_ms, float *x_ms, float *total
  * jobs' launch sequences; the GPU overlaps the jobs.  The reference runs one
  * FxKernel per sub-integration and thread (fxkernel/src/bench_fxkernel.cpp:93-139)
  * and has no batch API; this replaces that thread replication on one GPU.
- * inputs are device pointers (16-byte aligned); inputs and delays are fixed when
- * the batch is created (create a new batch to change them).  Creation runs every
+ * inputs are device pointers (16-byte aligned), or pinned host pointers: then each
+ * launch copies them host->device at the head of that job's graph branch, so the
+ * copies of some jobs overlap the correlation of others.  The input addresses and
+ * delays are fixed when the batch is created (the buffers' contents are read at
+ * every launch; create a new batch to change addresses or delays).  Creation runs every
  * job once.  Results: gxc_get_visibilities(gxc_batch_job(b, i), out) after the
  * launch's stream has completed. */
 typedef struct gxc_job {
   gxc_config cfg;
-  const uint8_t *const *inputs; /* [nant] device buffers */
+  const uint8_t *const *inputs; /* [nant] device buffers or pinned host buffers */
   const double *poly;           /* [nant][3] */
   const double *fso;            /* [nant] */
 } gxc_job;

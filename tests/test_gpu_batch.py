@@ -1,6 +1,7 @@
 """GPU tests of the batch API (uneven jobs in one graph launch) and the autotuner."""
 import numpy as np
 import pytest
+import torch
 
 from gcorr_gb300 import FxKernel, synth
 from gcorr_gb300.batch import Batch
@@ -59,3 +60,24 @@ def test_autotune_caches(tmp_path):
     assert r1["fft_block"] in (8, 24) and r1["x_engine"] in ("tensor", "cuda_core") and r1["tried"]
     r2 = tune(_job(w, d, precision="fp16"), blocks=(8, 24), path=path)
     assert r2 == r1
+
+
+def test_batch_on_pinned_host_inputs():
+    """Host inputs: each job's host->device copy is captured into its graph branch."""
+    data = [synth.random_bytes(w) for w in JOBS]
+    host = [[x.pin_memory() for x in d["inputs"]] for d in data]
+    dev = [[x.cuda() for x in d["inputs"]] for d in data]
+    bh = Batch([dict(_job(w, d, precision="fp16"), inputs=hx) for w, d, hx in zip(JOBS, data, host)])
+    bd = Batch([dict(_job(w, d, precision="fp16"), inputs=dx) for w, d, dx in zip(JOBS, data, dev)])
+    bh.launch()
+    bd.launch()
+    for i in range(len(JOBS)):
+        assert np.array_equal(bh.visibilities(i), bd.visibilities(i))
+    # the graph re-reads the host buffers on every launch
+    for hx in host:
+        for x in hx:
+            x.copy_(torch.randint(0, 256, x.shape, dtype=torch.uint8))
+    bh.launch()
+    assert not np.array_equal(bh.visibilities(0), bd.visibilities(0))
+    bh.close()
+    bd.close()
