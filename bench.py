@@ -369,7 +369,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gxcorr", choices=["gxcorr", "reference"])
     ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "fp8"])
     ap.add_argument("--x-engine", default="auto", choices=["auto", "cuda_core", "tensor"])
     ap.add_argument("--fft-block", type=int, default=0)
     ap.add_argument("--nfft", type=int, default=0, help="override the FFT count (small profiling captures)")
@@ -450,7 +450,7 @@ def main():
     xcmp = {}
     if not args.no_xcompare:
         for name, prec, eng in (("fp32_cuda_core", "fp32", "cuda_core"), ("fp32_tensor_split", "fp32", "tensor"),
-                                ("fp16_tensor", "fp16", "tensor")):
+                                ("fp16_tensor", "fp16", "tensor"), ("fp8_tensor", "fp8", "tensor")):
             try:
                 fy = G.FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=prec,
                                 rotator="exact", autos=True, x_engine=eng, fft_block=args.fft_block, device=local)
@@ -511,7 +511,7 @@ def main():
     # roofline of the dominant kernel, per launch: algorithmic bytes of one launch (units = FFTs
     # of all streams it processes) over that kernel's average launch duration in the timed step
     pk = peaks()
-    esz = 8 if args.precision == "fp32" else 4
+    esz = {"fp32": 8, "fp16": 4, "fp8": 2}[args.precision]
     in_bytes = w.bytes_per_antenna * w.nant
     chan_bytes = w.nant * 2 * w.nfft * w.nchan * esz
     nprod = 4 * w.nant * (w.nant + 1) // 2
@@ -554,7 +554,8 @@ def main():
         line = {
             "metric": "input Gsamples/s", "value": value, "unit": "input Gsamples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f16",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp32": "f32", "fp16": "f16", "fp8": "e4m3 data, f32 accumulate"}[args.precision],
             "data": "synthetic",
             "config": {"workload": CONFIGS[args.config][0], "nant": w.nant, "nchan": w.nchan, "nfft": w.nfft,
                        "fft_len": w.fft_len, "nbit": w.nbit, "precision": args.precision,

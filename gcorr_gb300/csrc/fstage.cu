@@ -214,6 +214,10 @@ template <> __device__ __forceinline__ float2 to_out<float2>(float2 v, float sca
 template <> __device__ __forceinline__ __half2 to_out<__half2>(float2 v, float scale) {
   return __floats2half2_rn(v.x * scale, v.y * scale);
 }
+// E4M3 pair, round to nearest, saturating at +-448 (re in the low byte)
+template <> __device__ __forceinline__ __nv_fp8x2_e4m3 to_out<__nv_fp8x2_e4m3>(float2 v, float scale) {
+  return __nv_fp8x2_e4m3(make_float2(v.x * scale, v.y * scale));
+}
 
 struct FParams {
   Job job;
@@ -757,6 +761,10 @@ cudaError_t launch_fstage(const Job &job, const float2 *twiddles, int t0, int nt
   prm.fsub_mask = job.fsub - 1;
   if (chan_type == CHAN_F32) {
     return job.is_complex ? launch_fstage_l<float2, true>(prm, nt, s) : launch_fstage_l<float2, false>(prm, nt, s);
+  }
+  if (chan_type == CHAN_F8) {
+    return job.is_complex ? launch_fstage_l<__nv_fp8x2_e4m3, true>(prm, nt, s)
+                          : launch_fstage_l<__nv_fp8x2_e4m3, false>(prm, nt, s);
   }
   return job.is_complex ? launch_fstage_l<__half2, true>(prm, nt, s) : launch_fstage_l<__half2, false>(prm, nt, s);
 }

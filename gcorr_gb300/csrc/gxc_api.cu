@@ -111,11 +111,10 @@ std::string validate(const gxc_config *c, gxc_status *st) {
   if (!((c->nbit == 2 && !c->is_complex) || (c->nbit == 8 && c->is_complex)))
     return "supported input formats: 2-bit real, 8-bit complex";
   if (!fstage_supported((int)F)) return "FFT length outside 256..32768";
-  if (c->precision == GXC_PRECISION_FP8) return "FP8 channelised data is not implemented";
   if (c->x_engine == GXC_XENGINE_TENSOR) {
-    const int ct = c->precision == GXC_PRECISION_FP32 ? CHAN_F32 : CHAN_F16;
-    if (!xstage_tensor_fits(c->nant, c->nchan, ct))
-      return "tensor-core X-stage: needs nant <= 64 (FP32 data: nant <= 32) and nchan a multiple of its channel tile";
+    if (!xstage_tensor_fits(c->nant, c->nchan, chan_type_of(c->precision)))
+      return "tensor-core X-stage: needs nant <= 64 (FP16), <= 32 (FP32, FP8) and nchan a multiple of its channel "
+             "tile";
   }
   *st = GXC_OK;
   return "";
@@ -220,7 +219,7 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   h->log2F = ilog2i(h->F);
   h->nbl = gxc_num_baselines(cfg);
   h->bytes_per_ant = input_bytes(cfg);
-  h->chan_type = (cfg->precision == GXC_PRECISION_FP32) ? CHAN_F32 : CHAN_F16;
+  h->chan_type = chan_type_of(cfg->precision);
   h->xeng = cfg->x_engine;
   // AUTO: tensor cores whenever the antenna count and channel tile fit.  FP32 data
   // uses the TF32 hi/lo split, whose TMEM accumulators are drained every 128
@@ -230,16 +229,19 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
     h->xeng = xstage_tensor_fits(nant, cfg->nchan, h->chan_type) ? GXC_XENGINE_TENSOR : GXC_XENGINE_CUDA_CORE;
   // FP16 storage keeps |X| near the sample rms: scale by 2^-floor(log2(F)/2),
   // an exact power of two undone exactly at finalisation.
-  if (h->chan_type == CHAN_F16) {
-    h->out_scale = ldexpf(1.0f, -(h->log2F / 2));
-    h->vis_scale = ldexpf(1.0f, 2 * (h->log2F / 2));
+  // FP8 (E4M3, largest finite 448) uses the same scale, and 2^-4 more for 8-bit data
+  // (sigma ~20 per component): the spectra then sit near rms 2..4, far from saturation.
+  if (h->chan_type != CHAN_F32) {
+    const int e = h->log2F / 2 + ((h->chan_type == CHAN_F8 && cfg->is_complex) ? 4 : 0);
+    h->out_scale = ldexpf(1.0f, -e);
+    h->vis_scale = ldexpf(1.0f, 2 * e);
   }
   // FFT block T (FFTs per F/X pass).  Every block adds its partial sums into the
   // compensated accumulators (read + write of sum and comp), so T is chosen large
   // enough that this traffic stays under ~6% of the channelised data of a block,
   // at least 4096 FFTs, and small enough for the device memory budget (40% of
   // the free memory, leaving room for inputs and the caller).
-  const size_t esz = h->chan_type == CHAN_F32 ? sizeof(float2) : sizeof(__half2);
+  const size_t esz = chan_elem_bytes(h->chan_type);
   const size_t per_fft = (size_t)cfg->nchan * 2 * nant * esz;
   int T = cfg->fft_block;
   if (T <= 0) {

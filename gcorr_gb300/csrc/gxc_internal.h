@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 #include <stdint.h>
 #include <stddef.h>
 
@@ -46,7 +47,12 @@ struct Job {
 };
 
 // Channelised-data element types.
-enum ChanType { CHAN_F32 = 0, CHAN_F16 = 1 };
+// FP8: E4M3 pairs (re, im), two bytes per complex value.
+enum ChanType { CHAN_F32 = 0, CHAN_F16 = 1, CHAN_F8 = 2 };
+inline size_t chan_elem_bytes(int chan_type) { return chan_type == CHAN_F32 ? 8 : chan_type == CHAN_F16 ? 4 : 2; }
+inline int chan_type_of(int precision) {
+  return precision == GXC_PRECISION_FP32 ? CHAN_F32 : precision == GXC_PRECISION_FP16 ? CHAN_F16 : CHAN_F8;
+}
 
 // fstage.cu
 cudaError_t launch_geometry(const Job &job, cudaStream_t s);

@@ -19,6 +19,7 @@ template <typename OutT>
 __device__ __forceinline__ OutT cvt(float2 v);
 template <> __device__ __forceinline__ float2 cvt<float2>(float2 v) { return v; }
 template <> __device__ __forceinline__ __half2 cvt<__half2>(float2 v) { return __floats2half2_rn(v.x, v.y); }
+template <> __device__ __forceinline__ __nv_fp8x2_e4m3 cvt<__nv_fp8x2_e4m3>(float2 v) { return __nv_fp8x2_e4m3(v); }
 
 // ants (gcorr layout) -> chan [ctile][T][nstream][CW] for FFTs [t0, t0+nt)
 template <typename OutT>
@@ -65,7 +66,7 @@ gxc_status xcorr_run(const float2 *ants, int nant, int nfft, int nchan, int fftw
   const int nstream = 2 * nant;
   const int nbl = nant * (nant - 1) / 2 + (autos ? nant : 0);
   const size_t nvis = (size_t)nbl * 4 * nchan;
-  const int ct = precision == GXC_PRECISION_FP32 ? CHAN_F32 : CHAN_F16;
+  const int ct = chan_type_of(precision);
   cudaError_t e = cudaMemsetAsync(vsum, 0, nvis * sizeof(float2), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(vcomp, 0, nvis * sizeof(float2), s);
   for (int t0 = 0; e == cudaSuccess && t0 < nfft; t0 += T) {
@@ -74,6 +75,9 @@ gxc_status xcorr_run(const float2 *ants, int nant, int nfft, int nchan, int fftw
     const unsigned blocks = (unsigned)((total + 255) / 256);
     if (ct == CHAN_F32)
       relayout_kernel<float2><<<blocks, 256, 0, s>>>(ants, nstream, nfft, nchan, fftwidth, t0, nt, T, (float2 *)chan);
+    else if (ct == CHAN_F8)
+      relayout_kernel<__nv_fp8x2_e4m3><<<blocks, 256, 0, s>>>(ants, nstream, nfft, nchan, fftwidth, t0, nt, T,
+                                                              (__nv_fp8x2_e4m3 *)chan);
     else
       relayout_kernel<__half2><<<blocks, 256, 0, s>>>(ants, nstream, nfft, nchan, fftwidth, t0, nt, T,
                                                       (__half2 *)chan);
@@ -100,16 +104,16 @@ gxc_status xcorr_check(int nant, int nfft, int nchan, int fftwidth, int precisio
     *msg = "gxc_xcorr: need nant >= 1, nfft >= 1, nchan >= 16 and a multiple of 16, fftwidth >= nchan";
     return GXC_ERR_INVALID_ARGUMENT;
   }
-  if (precision != GXC_PRECISION_FP32 && precision != GXC_PRECISION_FP16) {
-    *msg = "gxc_xcorr: precision must be FP32 or FP16";
-    return GXC_ERR_UNSUPPORTED;
+  if (precision != GXC_PRECISION_FP32 && precision != GXC_PRECISION_FP16 && precision != GXC_PRECISION_FP8) {
+    *msg = "gxc_xcorr: precision must be FP32, FP16 or FP8";
+    return GXC_ERR_INVALID_ARGUMENT;
   }
-  const int ct = precision == GXC_PRECISION_FP32 ? CHAN_F32 : CHAN_F16;
+  const int ct = chan_type_of(precision);
   const bool tc_ok = xstage_tensor_fits(nant, nchan, ct) != 0;
   if (*engine == GXC_XENGINE_AUTO) *engine = tc_ok ? GXC_XENGINE_TENSOR : GXC_XENGINE_CUDA_CORE;
   if (*engine == GXC_XENGINE_TENSOR && !tc_ok) {
-    *msg = "gxc_xcorr: the tensor-core X-stage needs nant <= 64 (FP32 data: nant <= 32) and nchan a multiple of "
-           "its channel tile";
+    *msg = "gxc_xcorr: the tensor-core X-stage needs nant <= 64 (FP16), <= 32 (FP32, FP8) and nchan a multiple "
+           "of its channel tile";
     return GXC_ERR_UNSUPPORTED;
   }
   return GXC_OK;
@@ -131,7 +135,7 @@ extern "C" gxc_status gxc_xcorr(const float *ants, int nant, int nfft, int nchan
   const int nbl = nant * (nant - 1) / 2 + (autos ? nant : 0);
   const size_t nvis = (size_t)nbl * 4 * nchan;
   const size_t nin = (size_t)2 * nant * nfft * fftwidth;
-  const size_t esz = precision == GXC_PRECISION_FP32 ? sizeof(float2) : sizeof(__half2);
+  const size_t esz = chan_elem_bytes(chan_type_of(precision));
   int T = nfft < 1024 ? nfft : 1024;
   // scratch: channelised block, accumulators, device copies of host buffers
   void *chan = nullptr;

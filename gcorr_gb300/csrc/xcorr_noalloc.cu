@@ -67,6 +67,7 @@ template <typename OutT>
 __device__ __forceinline__ OutT cvt(float2 v);
 template <> __device__ __forceinline__ float2 cvt<float2>(float2 v) { return v; }
 template <> __device__ __forceinline__ __half2 cvt<__half2>(float2 v) { return __floats2half2_rn(v.x, v.y); }
+template <> __device__ __forceinline__ __nv_fp8x2_e4m3 cvt<__nv_fp8x2_e4m3>(float2 v) { return __nv_fp8x2_e4m3(v); }
 
 // ants[(ant*2+pol)*nfft*fftwidth + f*fftwidth + c] -> [ctile][T][stream][16] for FFTs [t0, t0+nt)
 template <typename OutT>
@@ -123,8 +124,8 @@ extern "C" gxc_status gxc_xcorr_noalloc(const float *ants, int nant, int nfft, i
   const int npairs = nat * (nat + 1) / 2;
   const int nbl = nant * (nant - 1) / 2 + (autos ? nant : 0);
   const size_t nvis = (size_t)nbl * 4 * nchan;
-  const size_t esz = precision == GXC_PRECISION_FP32 ? sizeof(float2) : sizeof(__half2);
-  const int ct = precision == GXC_PRECISION_FP32 ? CHAN_F32 : CHAN_F16;
+  const size_t esz = chan_elem_bytes(chan_type_of(precision));
+  const int ct = chan_type_of(precision);
   // scratch layout: [pair table][sum][comp][channelised block of T FFTs]
   const size_t off_sum = align256(sizeof(int2) * (size_t)npairs);
   const size_t off_comp = off_sum + align256(sizeof(float2) * nvis);

@@ -21,6 +21,9 @@ namespace gxc {
 template <typename InT> __device__ __forceinline__ float2 ld_c(const InT *p);
 template <> __device__ __forceinline__ float2 ld_c<float2>(const float2 *p) { return *p; }
 template <> __device__ __forceinline__ float2 ld_c<__half2>(const __half2 *p) { return __half22float2(*p); }
+template <> __device__ __forceinline__ float2 ld_c<__nv_fp8x2_e4m3>(const __nv_fp8x2_e4m3 *p) {
+  return static_cast<float2>(*p);
+}
 
 // x * conj(y) accumulated into a
 __device__ __forceinline__ void cmac_conj(float2 &a, float2 x, float2 y) {
@@ -145,7 +148,7 @@ cudaError_t launch_xstage_cuda_core_pairs(const void *chan, int chan_type, int n
   const int nat = (nant + 1) / 2;
   const int npairs = nat * (nat + 1) / 2;
   const int nstream = 2 * nant;
-  const size_t esz = chan_type == CHAN_F32 ? sizeof(float2) : sizeof(__half2);
+  const size_t esz = chan_elem_bytes(chan_type);
   const int pairs_per_cta = npairs < 64 ? npairs : 64;
   const int threads = pairs_per_cta * CW;
   int TT = (int)(65536 / ((size_t)nstream * CW * esz));
@@ -160,6 +163,12 @@ cudaError_t launch_xstage_cuda_core_pairs(const void *chan, int chan_type, int n
     if (e != cudaSuccess) return e;
     k<<<grid, threads, smem, s>>>((const float2 *)chan, nant, nchan, T, nt, autos, pairs, npairs, pairs_per_cta, TT,
                                    vsum, vcomp);
+  } else if (chan_type == CHAN_F8) {
+    auto k = xstage_cc_kernel<__nv_fp8x2_e4m3>;
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, threads, smem, s>>>((const __nv_fp8x2_e4m3 *)chan, nant, nchan, T, nt, autos, pairs, npairs,
+                                   pairs_per_cta, TT, vsum, vcomp);
   } else {
     auto k = xstage_cc_kernel<__half2>;
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -143,6 +143,18 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64
       : "memory");
 }
 
+// D[tmem] (+)= A[smem] * B[smem]^T, kind::f8f6f4 with A = B = E4M3 (instruction
+// descriptor format codes 0), FP32 accumulate; K = 32 one-byte elements per MMA.
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 // Arrives on the mbarrier once every previously issued tcgen05.mma of this thread completed.
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
@@ -194,11 +206,15 @@ struct Params {
   int *err;
 };
 
-// FP16 path: one accumulation over the whole FFT block (its TMEM rounding bias,
-// ~1e-5 over 2048 FFTs, is far below the FP16 quantisation error).
+// FP16 and FP8 paths: one accumulation over the whole FFT block (its TMEM rounding
+// bias, ~1e-5 over 2048 FFTs, is far below the FP16 / FP8 quantisation error).
+// A 128-byte SW128 row holds 64 FFTs of FP16 or 128 FFTs of FP8 (E4M3) values;
+// either way one MMA consumes 32 bytes of every row (K = 16 or 32).
+template <bool F8>
 __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
   using C = Cfg<false>;
-  constexpr int KC = C::KC, NG = C::NG, GROUP_BYTES = C::GROUP_BYTES, STAGE_BYTES = C::STAGE_BYTES;
+  constexpr int KC = F8 ? 128 : C::KC, KSTEP = F8 ? 32 : C::KSTEP;
+  constexpr int NG = C::NG, GROUP_BYTES = C::GROUP_BYTES, STAGE_BYTES = C::STAGE_BYTES;
   constexpr int TMEM_COLS = C::TMEM_COLS;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_done;
@@ -264,7 +280,44 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
           const int rest = task / nq;
           const int s = rest % n;
           const int o = rest / n;
-          {
+          if constexpr (F8) {
+            const int c = cb + 4 * q;
+            const int ctile = c >> 4, coff = c & 15;
+            // 16 FFTs x 4 channels of E4M3 pairs (8 bytes per FFT) -> 8 rows (4 channels x re/im)
+            // of 16 FFT bytes: two prmt gather one channel's (re, im) bytes of 2 FFTs each, a
+            // third and fourth split them into 4 re bytes and 4 im bytes
+            const __nv_fp8x2_e4m3 *src =
+                (const __nv_fp8x2_e4m3 *)p.chan + ((size_t)ctile * p.T * n + s) * CW + coff;
+            uint2 v[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+              const int t = tb + 16 * o + i;
+              v[i] = (t < p.nt) ? __ldg(reinterpret_cast<const uint2 *>(src + (size_t)t * n * CW))
+                                : make_uint2(0, 0);
+            }
+#pragma unroll
+            for (int ci = 0; ci < 4; ci++) {
+              const int cc = 4 * q + ci;
+              const int G = cc / p.g, gi = cc - G * p.g;
+              const int row = gi * p.R + 2 * s;
+              const uint32_t sel = (ci & 1) ? 0x7362u : 0x5140u;
+              uint32_t re[4], im[4];
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                const uint32_t a0 = (ci < 2) ? v[4 * k].x : v[4 * k].y, a1 = (ci < 2) ? v[4 * k + 1].x : v[4 * k + 1].y;
+                const uint32_t a2 = (ci < 2) ? v[4 * k + 2].x : v[4 * k + 2].y;
+                const uint32_t a3 = (ci < 2) ? v[4 * k + 3].x : v[4 * k + 3].y;
+                const uint32_t t0 = prmt(a0, a1, sel), t1 = prmt(a2, a3, sel);
+                re[k] = prmt(t0, t1, 0x5410);
+                im[k] = prmt(t0, t1, 0x7632);
+              }
+              unsigned char *gbase = stage + G * GROUP_BYTES;
+              *reinterpret_cast<uint4 *>(gbase + row * 128 + ((o ^ (row & 7)) << 4)) =
+                  make_uint4(re[0], re[1], re[2], re[3]);
+              *reinterpret_cast<uint4 *>(gbase + (row + 1) * 128 + ((o ^ ((row + 1) & 7)) << 4)) =
+                  make_uint4(im[0], im[1], im[2], im[3]);
+            }
+          } else {
             const int c = cb + 4 * q;
             const int ctile = c >> 4, coff = c & 15;
             // 8 FFTs x 4 channels of FP16 complex -> 8 rows (4 channels x re/im) of 8 FFTs
@@ -309,10 +362,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
 #pragma unroll
       for (int G = 0; G < NG; G++) {
 #pragma unroll
-        for (int kk = 0; kk < KC / C::KSTEP; kk++) {
+        for (int kk = 0; kk < KC / KSTEP; kk++) {
           const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
           const uint64_t dh = desc_sw128(sa + G * GROUP_BYTES + kk * 32);
-          mma_f16(tmem + G * 128, dh, dh, IDESC, acc);
+          if constexpr (F8) mma_f8(tmem + G * 128, dh, dh, IDESC, acc);
+          else mma_f16(tmem + G * 128, dh, dh, IDESC, acc);
         }
       }
       mma_commit(smem_u32(&bar_empty[st]));
@@ -639,8 +693,9 @@ constexpr int BIG_STAGES = 4;
 constexpr int BIG_STAGE_BYTES = 256 * 128;
 constexpr uint32_t IDESC_N256 = (1u << 4) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
 
+template <bool F8>
 __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big_kernel(Params p) {
-  constexpr int KC = 64;
+  constexpr int KC = F8 ? 128 : 64, KSTEP = F8 ? 32 : 16;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_full[BIG_STAGES], bar_empty[BIG_STAGES], bar_done;
   __shared__ uint32_t tmem_base_sh;
@@ -679,9 +734,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big_kernel(Params p) {
   const uint32_t tmem = tmem_base_sh;
 
   if (warp < NPROD_WARPS) {
-    // task = (stream s, 16-byte K chunk o): 8 FFTs of one stream of this channel
+    // task = (stream s, 16-byte K chunk o): 8 FFTs (FP16) or 16 FFTs (FP8) of one stream of this channel
     const int ntask = 8 * n;
-    const __half2 *src = (const __half2 *)p.chan + ((size_t)(c >> 4) * p.T * n) * CW + (c & 15);
+    const size_t esz = F8 ? 2 : 4;
+    const unsigned char *src = (const unsigned char *)p.chan + (((size_t)(c >> 4) * p.T * n) * CW + (c & 15)) * esz;
     for (int ch = 0; ch < nchunks; ch++) {
       const int st = ch % BIG_STAGES;
       if (ch >= BIG_STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / BIG_STAGES) - 1) & 1, p.err)) break;
@@ -690,16 +746,38 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big_kernel(Params p) {
       for (int task = tid; task < ntask; task += NPROD) {
         const int s = task % n;
         const int o = task / n;
-        uint32_t w[8];
+        uint4 re, im;
+        if constexpr (F8) {
+          // 16 E4M3 pairs (re low byte, im high byte) -> 16 re bytes and 16 im bytes
+          uint32_t w[8];
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-          const int t = tb + 8 * o + i;
-          w[i] = (t < p.nt) ? __ldg(reinterpret_cast<const uint32_t *>(src + ((size_t)t * n + s) * CW)) : 0u;
+          for (int i = 0; i < 8; i++) {
+            uint32_t h2[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+              const int t = tb + 16 * o + 2 * i + h;
+              h2[h] = (t < p.nt) ? (uint32_t)__ldg(reinterpret_cast<const unsigned short *>(
+                                       src + ((size_t)t * n + s) * CW * esz))
+                                 : 0u;
+            }
+            w[i] = h2[0] | (h2[1] << 16);  // re(2i), im(2i), re(2i+1), im(2i+1)
+          }
+          re = make_uint4(prmt(w[0], w[1], 0x6420), prmt(w[2], w[3], 0x6420), prmt(w[4], w[5], 0x6420),
+                          prmt(w[6], w[7], 0x6420));
+          im = make_uint4(prmt(w[0], w[1], 0x7531), prmt(w[2], w[3], 0x7531), prmt(w[4], w[5], 0x7531),
+                          prmt(w[6], w[7], 0x7531));
+        } else {
+          uint32_t w[8];
+#pragma unroll
+          for (int i = 0; i < 8; i++) {
+            const int t = tb + 8 * o + i;
+            w[i] = (t < p.nt) ? __ldg(reinterpret_cast<const uint32_t *>(src + ((size_t)t * n + s) * CW * esz)) : 0u;
+          }
+          re = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410), prmt(w[4], w[5], 0x5410),
+                          prmt(w[6], w[7], 0x5410));
+          im = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632), prmt(w[4], w[5], 0x7632),
+                          prmt(w[6], w[7], 0x7632));
         }
-        const uint4 re = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410), prmt(w[4], w[5], 0x5410),
-                                    prmt(w[6], w[7], 0x5410));
-        const uint4 im = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632), prmt(w[4], w[5], 0x7632),
-                                    prmt(w[6], w[7], 0x7632));
         const int row = 2 * s;
         *reinterpret_cast<uint4 *>(stage + row * 128 + ((o ^ (row & 7)) << 4)) = re;
         *reinterpret_cast<uint4 *>(stage + (row + 1) * 128 + ((o ^ ((row + 1) & 7)) << 4)) = im;
@@ -714,12 +792,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big_kernel(Params p) {
       tc_fence_after();
       const uint32_t sa = sbase + st * BIG_STAGE_BYTES;
 #pragma unroll
-      for (int kk = 0; kk < KC / 16; kk++) {
+      for (int kk = 0; kk < KC / KSTEP; kk++) {
         const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
         const uint64_t dall = desc_sw128(sa + kk * 32);            // rows 0..255 (also the top half's A)
         const uint64_t dbot = desc_sw128(sa + 128 * 128 + kk * 32);  // rows 128..255
-        mma_f16(tmem, dall, dall, IDESC_N256, acc);                // D_top: rows 0..127 x cols 0..255
-        mma_f16(tmem + 256, dbot, dbot, IDESC, acc);               // D_bot: rows 128..255 x cols 128..255
+        if constexpr (F8) {
+          mma_f8(tmem, dall, dall, IDESC_N256, acc);
+          mma_f8(tmem + 256, dbot, dbot, IDESC, acc);
+        } else {
+          mma_f16(tmem, dall, dall, IDESC_N256, acc);                // D_top: rows 0..127 x cols 0..255
+          mma_f16(tmem + 256, dbot, dbot, IDESC, acc);               // D_bot: rows 128..255 x cols 128..255
+        }
       }
       mma_commit(smem_u32(&bar_empty[st]));
     }
@@ -782,7 +865,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big_kernel(Params p) {
 }  // namespace tc
 
 // two rows (re, im) per stream, two streams per antenna: up to 32 antennas fill one
-// M = 128 tile per channel; 33..64 antennas use the split-M kernel (FP16 only)
+// M = 128 tile per channel; 33..64 antennas use the split-M kernel (FP16 or FP8)
 int xstage_tensor_supported(int nant) { return nant >= 1 && 4 * nant <= 256; }
 
 static int g_err_dev = -1;
@@ -816,7 +899,7 @@ cudaError_t xstage_tensor_take_error(int *flag) {
 
 // Channels per CTA of the tensor-core X-stage for nant antennas (the channel count must divide by it).
 int xstage_tensor_channels_per_cta(int nant, int chan_type) {
-  if (4 * nant > 128) return chan_type == CHAN_F32 ? 0 : 1;  // split-M kernel: one channel, FP16 only
+  if (4 * nant > 128) return chan_type == CHAN_F32 ? 0 : 1;  // split-M kernel: one channel, FP16 or FP8
   int R = 16;
   while (R < 4 * nant) R <<= 1;  // 2 rows (re, im) per stream, 2 streams per antenna
   return (chan_type == CHAN_F32 ? tc::Cfg<true>::NG : tc::Cfg<false>::NG) * (128 / R);
@@ -855,9 +938,10 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   static_assert(tc::Cfg<true>::STAGE_BYTES == 65536 && tc::Cfg<false>::STAGE_BYTES == 65536, "stage size");
   if (R > 128) {
     const size_t bsmem = (size_t)tc::BIG_STAGES * tc::BIG_STAGE_BYTES + 1024;
-    e = cudaFuncSetAttribute(tc::xstage_tc_big_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
+    auto kern = chan_type == CHAN_F8 ? tc::xstage_tc_big_kernel<true> : tc::xstage_tc_big_kernel<false>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
     if (e != cudaSuccess) return e;
-    tc::xstage_tc_big_kernel<<<nchan, tc::NTHREADS, bsmem, s>>>(p);
+    kern<<<nchan, tc::NTHREADS, bsmem, s>>>(p);
   } else if (chan_type == CHAN_F32) {
     auto launch = [&](auto kern) -> cudaError_t {
       cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -874,9 +958,10 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
     }
     if (e != cudaSuccess) return e;
   } else {
-    e = cudaFuncSetAttribute(tc::xstage_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = chan_type == CHAN_F8 ? tc::xstage_tc_kernel<true> : tc::xstage_tc_kernel<false>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    tc::xstage_tc_kernel<<<nchan / p.CS, tc::NTHREADS, smem, s>>>(p);
+    kern<<<nchan / p.CS, tc::NTHREADS, smem, s>>>(p);
   }
   return cudaGetLastError();
 }
