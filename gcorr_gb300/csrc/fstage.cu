@@ -35,18 +35,33 @@ __global__ void geometry_kernel(Job job) {
   const double mean = __dadd_rn(__dmul_rn(a, 0.5), b);
   const double ndf = __ddiv_rn(__dsub_rn(mean, fso), job.Ts);
   Geom g;
-  g.a = a;
-  g.b = b;
-  g.frac = 0.0;
+  g.c0 = g.c1 = g.cstep = g.cf = 0.0f;
   g.offset = 0;
   g.valid = 0;
+  g.pad[0] = g.pad[1] = 0;
   if (fabs(ndf) < 1.0e9) {  // false for NaN/Inf: flagged instead of undefined int()
     const int nd = __double2int_rz(__dadd_rn(ndf, 0.5));
     double frac = -__dmul_rn(__dsub_rn(ndf, (double)nd), job.Ts);
     long long off = (long long)i * job.F - nd;
     if (off == -1) { off++; frac = __dadd_rn(frac, job.Ts); }
     if (off == job.maxoffset + 1) { off--; frac = __dsub_rn(frac, job.Ts); }
-    g.frac = frac;
+    // Phase constants (fxkernel.cpp:503-535): phase(n) = LO*(b + a*n/F) turns, the
+    // integer-sample part of b removed and the rest reduced mod 1 turn in FP64.
+    const int intdelay = __double2int_rz(b);
+    const double br = b - (double)intdelay;
+    double c0 = br * job.lo_hz;
+    if (job.fractional_lo) c0 += (job.lo_hz - trunc(job.lo_hz)) * (double)intdelay;
+    c0 -= floor(c0);
+    const double c1 = a * job.lo_hz / (double)job.F;  // turns per sample
+    // coarse step: the reference advances its step table by `stride` samples per
+    // entry (fxkernel.cpp:112) while applying it every `substride` samples;
+    // FXKERNEL mode keeps that, EXACT uses the true step.
+    const double stepmul = (job.rotator == GXC_ROTATOR_FXKERNEL) ? (double)job.stride : (double)job.substride;
+    g.c0 = (float)c0;
+    g.c1 = (float)c1;
+    g.cstep = (float)(c1 * stepmul);
+    // fractional-sample correction exp(+2 pi i c bw/nchan frac) (fxkernel.cpp:171-175,600-630)
+    g.cf = (float)(job.bw_hz / (double)job.nchan * frac);
     if (off >= 0 && off <= job.maxoffset) {
       g.offset = (int)off;
       g.valid = 1;
@@ -307,6 +322,15 @@ __device__ __forceinline__ void twiddle(float2 *u, int k, const float2 *__restri
   }
 }
 
+// 16-byte asynchronous global -> shared copy (LDGSTS, bypassing L1); completion
+// is awaited with cp.async.wait_all before the barrier that publishes the data.
+__device__ __forceinline__ void cp_async16(void *dst_smem, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst_smem)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 template <int L, typename OutT, bool CPLX>
 __global__ void __launch_bounds__(FPlan<L, CPLX>::NT, FPlan<L, CPLX>::MINB) fstage_kernel(FParams prm) {
   using Pl = FPlan<L, CPLX>;
@@ -321,44 +345,19 @@ __global__ void __launch_bounds__(FPlan<L, CPLX>::NT, FPlan<L, CPLX>::MINB) fsta
   float2 *fsubt = tstep + STRIDE;         // frac-delay, fine part [FSUB]
   float2 *fstept = fsubt + FSUB;          // frac-delay, coarse part [STRIDE]
   unsigned char *stage = reinterpret_cast<unsigned char *>(fstept + STRIDE);  // packed input window
-  __shared__ Geom g;
-  __shared__ float cst[4];
-  __shared__ long long stage_base;
 
-  const int tl = blockIdx.x;
+  // grid x = pol + 2 * FFT: the two pols of one window run side by side (the second
+  // read of the packed window hits L2) and write neighbouring streams
+  const int pol = blockIdx.x & 1;  // the pol this CTA transforms
+  const int tl = blockIdx.x >> 1;
   const int ant = blockIdx.y;
-  const int pol = blockIdx.z;  // the pol this CTA transforms
   const int t = prm.t0 + tl;
   const int tid = threadIdx.x;
   const int nstreams = 2 * job.nant;
   const int s = 2 * ant + pol;
   OutT *chan = reinterpret_cast<OutT *>(prm.chan);
-
-  if (tid == 0) {
-    g = job.geom[(size_t)ant * job.nfft + t];
-    if (g.valid) {
-      // Per-FFT FP64 constants, reduced mod 1 turn before going to FP32
-      // (fxkernel.cpp:503-535): phase(n) = LO*(b + a*n/F) turns.
-      const int intdelay = __double2int_rz(g.b);
-      const double br = g.b - (double)intdelay;
-      double c0 = br * job.lo_hz;
-      if (job.fractional_lo) c0 += (job.lo_hz - trunc(job.lo_hz)) * (double)intdelay;
-      c0 -= floor(c0);
-      const double c1 = g.a * job.lo_hz / (double)N;  // turns per sample
-      // coarse step: the reference advances its step table by `stride` samples
-      // per entry (fxkernel.cpp:112) while applying it every `substride` samples;
-      // FXKERNEL mode keeps that, EXACT uses the true step.
-      const double stepmul = (job.rotator == GXC_ROTATOR_FXKERNEL) ? (double)STRIDE : (double)SUB;
-      cst[0] = (float)c0;
-      cst[1] = (float)c1;
-      cst[2] = (float)(c1 * stepmul);
-      // fractional-sample correction: exp(+2 pi i c bw/nchan frac) (fxkernel.cpp:171-175,600-630)
-      cst[3] = (float)(job.bw_hz / (double)NCHAN * g.frac);  // turns per channel
-      const long long first = CPLX ? 4LL * g.offset : ((long long)g.offset >> 1);
-      stage_base = first & ~15LL;
-    }
-  }
-  __syncthreads();
+  // every thread reads the 32-byte record (one broadcast load): no barrier needed
+  const Geom g = job.geom[(size_t)ant * job.nfft + t];
 
   // channelised layout [ctile][t][stream][16]: element (c, s) of this FFT
   OutT *out0 = chan + ((size_t)tl * nstreams + s) * CW;
@@ -371,6 +370,7 @@ __global__ void __launch_bounds__(FPlan<L, CPLX>::NT, FPlan<L, CPLX>::MINB) fsta
     return;
   }
 
+  const long long stage_base = (CPLX ? 4LL * g.offset : ((long long)g.offset >> 1)) & ~15LL;
   {
     // stage the packed window with 16-byte loads (bounds: the buffer holds
     // (nfft+1)*F samples and offset <= (nfft-1)*F, so the window plus the
@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(FPlan<L, CPLX>::NT, FPlan<L, CPLX>::MINB) fsta
     const int nvec = (int)((last - stage_base + 15) >> 4);
     uint4 *dst = reinterpret_cast<uint4 *>(stage);
     for (int i = tid; i < nvec; i += NT) dst[i] = __ldg(&src[i]);
-    const float c0 = cst[0], c1 = cst[1], cstep = cst[2], cf = cst[3];
+    const float c0 = g.c0, c1 = g.c1, cstep = g.cstep, cf = g.cf;
     for (int k = tid; k < SUB; k += NT) {
       float sn, cs;
       sincospif(-2.0f * fmaf((float)k, c1, c0), &sn, &cs);
@@ -436,8 +436,8 @@ __global__ void __launch_bounds__(FPlan<L, CPLX>::NT, FPlan<L, CPLX>::MINB) fsta
       dft<R0>(v);
     }
   }
-  __syncthreads();  // (the staged window and tables stay in place; nothing else to wait for)
-  // store pass 0: element j + r with j = iv*R0, padded index iv*(R0+1) + r
+  // store pass 0: element j + r with j = iv*R0, padded index iv*(R0+1) + r (buf is
+  // not read before the next barrier)
   if (active) {
 #pragma unroll
     for (int q = 0; q < 32 / R0; q++) {
@@ -519,7 +519,7 @@ static cudaError_t launch_fstage_t(const FParams &prm, int nt, cudaStream_t s) {
   auto kern = fstage_kernel<L, OutT, CPLX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)nt, (unsigned)job.nant, 2u);
+  dim3 grid(2u * (unsigned)nt, (unsigned)job.nant, 1u);
   kern<<<grid, Pl::NT, smem, s>>>(prm);
   return cudaGetLastError();
 }
@@ -529,20 +529,33 @@ static cudaError_t launch_fstage_t(const FParams &prm, int nt, cudaStream_t s) {
 // so a cluster of two CTAs shares it (four-step factorisation N = 128 x 256):
 //   step 1: CTA r takes columns n2 in [128r, 128r+128): 128-point FFTs over n1
 //           of x[256 n1 + n2] (radix 32 then 4), decoded and fringe-rotated
-//           straight from global memory, times the twiddle W_N^(n2 k1);
+//           from a staged copy of its 128 rows of the packed window, times the
+//           twiddle W_N^(n2 k1);
 //   step 2: after a cluster barrier, CTA r reads rows k1 in [64r, 64r+64) of
 //           both CTAs' [k1][n2] buffers (half through distributed shared memory);
 //   step 3: after a second cluster barrier, 256-point FFTs over n2 (radix 16 x 16)
 //           give X[k1 + 128 k2], multiplied by the frac-delay phase and stored.
+// Every twiddle is W_N^e = Thi[e >> 7] * Tlo[e & 127] from two shared tables
+// (Thi[h] = W_N^(128 h), Tlo[l] = W_N^l), so no pass gathers from the N-entry table.
+// Grid x = rank + 2 * (pol + 2 * FFT): the two pols of one window are neighbouring
+// clusters (the second read of the window hits L2) and write neighbouring streams.
 // The flagged-window path returns before any cluster barrier, in both CTAs alike.
 constexpr int F15 = 32768;
 constexpr int F15_STRIDE = 128;                 // fringe/frac table split (2^floor(log2 nchan / 2))
 constexpr int F15_SUB = F15 / F15_STRIDE;       // 256
 constexpr int F15_BUF = 64 * 272;               // complex slots: max(128x129, 128x132, 64x272)
+// staged rows: 128 samples of one row n1 (4 bytes each for 8-bit complex, 2 bits per
+// pol for 2-bit real) plus the 16-byte rounding of the row start
+template <bool CPLX> struct F15Stage {
+  static constexpr int ROW = CPLX ? 512 + 16 : 64 + 16;  // bytes per staged row (16-byte multiple)
+  static constexpr int CHUNKS = ROW / 16;
+  static constexpr int BYTES = 128 * ROW;
+};
 
 template <typename OutT, bool CPLX>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_cluster_kernel(FParams prm) {
   namespace cg = cooperative_groups;
+  using St = F15Stage<CPLX>;
   constexpr int NCHAN = CPLX ? F15 : F15 / 2;
   constexpr int FSUB = NCHAN / F15_STRIDE;
   const Job &job = prm.job;
@@ -553,13 +566,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_clust
   float2 *tstep = tsub + F15_SUB;           // [F15_STRIDE]
   float2 *fsubt = tstep + F15_STRIDE;       // [FSUB]
   float2 *fstept = fsubt + FSUB;            // [F15_STRIDE]
+  float2 *thi = fstept + F15_STRIDE;        // [256] W_N^(128 h)
+  float2 *tlo = thi + 256;                  // [128] W_N^l
+  unsigned char *stage = reinterpret_cast<unsigned char *>(tlo + 128);  // [128][St::ROW]
   __shared__ Geom g;
-  __shared__ float cst[4];
 
   const int rk = (int)cluster.block_rank();
-  const int tl = blockIdx.x >> 1;
+  const int pol = (blockIdx.x >> 1) & 1;
+  const int tl = blockIdx.x >> 2;
   const int ant = blockIdx.y;
-  const int pol = blockIdx.z;
   const int t = prm.t0 + tl;
   const int tid = threadIdx.x;
   const int nstreams = 2 * job.nant;
@@ -569,22 +584,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_clust
   const size_t ctile_stride = (size_t)prm.T * nstreams * CW;
   const float2 *__restrict__ tw = prm.tw;
 
-  if (tid == 0) {
-    g = job.geom[(size_t)ant * job.nfft + t];
-    if (g.valid) {
-      const int intdelay = __double2int_rz(g.b);
-      const double br = g.b - (double)intdelay;
-      double c0 = br * job.lo_hz;
-      if (job.fractional_lo) c0 += (job.lo_hz - trunc(job.lo_hz)) * (double)intdelay;
-      c0 -= floor(c0);
-      const double c1 = g.a * job.lo_hz / (double)F15;
-      const double stepmul = (job.rotator == GXC_ROTATOR_FXKERNEL) ? (double)F15_STRIDE : (double)F15_SUB;
-      cst[0] = (float)c0;
-      cst[1] = (float)c1;
-      cst[2] = (float)(c1 * stepmul);
-      cst[3] = (float)(job.bw_hz / (double)NCHAN * g.frac);
-    }
-  }
+  if (tid == 0) g = job.geom[(size_t)ant * job.nfft + t];
   __syncthreads();
   if (!g.valid) {  // both CTAs of the cluster see the same record
     const OutT z = to_out<OutT>(make_float2(0.f, 0.f), 1.f);
@@ -592,8 +592,23 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_clust
       out0[(size_t)(c >> 4) * ctile_stride + (c & 15)] = z;
     return;
   }
+  const long long off = g.offset;
+  // stage rows n1 = 0..127 of this CTA's columns: samples off + 256 n1 + 128 rk + [0, 128)
+  // (bounds: offset <= (nfft-1)*F and the buffer holds (nfft+1)*F samples, so the row
+  // ends, rounded up to 16 bytes, stay inside it)
+  const long long row0 = CPLX ? 4 * (off + 128 * rk) : ((off + 128 * rk) >> 1);
+  const long long rbase = row0 & ~15LL;   // row n1 starts at rbase + n1 * (1024 or 128) bytes
+  const int mis = (int)(row0 - rbase);
   {
-    const float c0 = cst[0], c1 = cst[1], cstep = cst[2], cf = cst[3];
+    const unsigned char *src = job.inputs[ant] + rbase;
+    constexpr long long RSTEP = CPLX ? 1024 : 128;
+    for (int j = tid; j < 128 * St::CHUNKS; j += 512) {
+      const int n1 = j / St::CHUNKS, c = j - n1 * St::CHUNKS;
+      cp_async16(stage + n1 * St::ROW + 16 * c, src + n1 * RSTEP + 16 * c);
+    }
+  }
+  {
+    const float c0 = g.c0, c1 = g.c1, cstep = g.cstep, cf = g.cf;
     for (int k = tid; k < F15_SUB; k += 512) {
       float sn, cs;
       sincospif(-2.0f * fmaf((float)k, c1, c0), &sn, &cs);
@@ -611,7 +626,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_clust
       sincospif(2.0f * ((float)k * cf), &sn, &cs);
       fsubt[k] = make_float2(cs, sn);
     }
+    if (tid < 256) thi[tid] = __ldg(&tw[128 * tid]);
+    else if (tid < 384) tlo[tid - 256] = __ldg(&tw[tid - 256]);
   }
+  cp_async_wait_all();
   __syncthreads();
 
   float2 u[32];
@@ -619,20 +637,20 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_clust
   const int col = tid & 127, iv = tid >> 7;
   const int n2 = 128 * rk + col;
   {
-    const uint8_t *in = job.inputs[ant];
-    const long long off = g.offset;
     const float2 rs = tsub[n2];  // n mod 256 = n2
-    const int shift = 2 * (2 * (int)((off + n2) & 1) + pol);
+    // 2-bit: sample off + 256 n1 + n2 sits in byte (that >> 1) = rbase + 128 n1 + mis + (p >> 1)
+    const int p = (int)(off & 1) + col;
+    const int shift = 2 * (2 * (p & 1) + pol);
 #pragma unroll
     for (int r = 0; r < 32; r++) {
       const int n1 = iv + 4 * r;
-      const long long m = off + 256LL * n1 + n2;
       const float2 rot = cmul(rs, tstep[n1]);
+      const unsigned char *row = stage + n1 * St::ROW + mis;
       if constexpr (CPLX) {
-        const char2 x = __ldg(reinterpret_cast<const char2 *>(in + 4 * m + 2 * pol));
+        const char2 x = *reinterpret_cast<const char2 *>(row + 4 * col + 2 * pol);
         u[r] = cmul(make_float2((float)x.x, (float)x.y), rot);
       } else {
-        const int byte = __ldg(in + (m >> 1));
+        const int byte = row[p >> 1];
         const float lv = level2bit((byte >> shift) & 3);
         u[r] = make_float2(lv * rot.x, lv * rot.y);
       }
@@ -650,10 +668,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_clust
 #pragma unroll
     for (int r = 0; r < 4; r++) v[r] = buf[col * 129 + ivb + 32 * r];
 #pragma unroll
-    for (int r = 1; r < 4; r++) v[r] = cmul(v[r], __ldg(&tw[r * ivb * (F15 / 128)]));
+    for (int r = 1; r < 4; r++) v[r] = cmul(v[r], thi[2 * r * ivb]);  // W_N^(256 r ivb)
     dft<4>(v);
 #pragma unroll
-    for (int r = 0; r < 4; r++) v[r] = cmul(v[r], __ldg(&tw[n2 * (ivb + 32 * r)]));
+    for (int r = 0; r < 4; r++) {
+      const int e = n2 * (ivb + 32 * r);  // < 256 * 128
+      v[r] = cmul(v[r], cmul(thi[e >> 7], tlo[e & 127]));
+    }
   }
   __syncthreads();
 #pragma unroll
@@ -695,7 +716,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_clust
 #pragma unroll
     for (int r = 0; r < 16; r++) v[r] = buf[kr * 272 + ivd + 17 * r];
 #pragma unroll
-    for (int r = 1; r < 16; r++) v[r] = cmul(v[r], __ldg(&tw[r * ivd * (F15 / 256)]));
+    for (int r = 1; r < 16; r++) v[r] = cmul(v[r], thi[r * ivd]);  // W_N^(128 r ivd)
     dft<16>(v);
 #pragma unroll
     for (int r = 0; r < RKEEP; r++) {
@@ -713,11 +734,12 @@ static cudaError_t launch_fstage_cluster(const FParams &prm, int nt, cudaStream_
   if (job.F != F15 || job.nchan != NCHAN || job.stride != F15_STRIDE || job.substride != F15_SUB ||
       job.fsub != NCHAN / F15_STRIDE)
     return cudaErrorInvalidValue;
-  const size_t smem = sizeof(float2) * ((size_t)F15_BUF + F15_SUB + 2 * F15_STRIDE + NCHAN / F15_STRIDE);
+  const size_t smem = sizeof(float2) * ((size_t)F15_BUF + F15_SUB + 2 * F15_STRIDE + NCHAN / F15_STRIDE + 256 + 128) +
+                      F15Stage<CPLX>::BYTES;
   auto kern = fstage_cluster_kernel<OutT, CPLX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  dim3 grid(2u * (unsigned)nt, (unsigned)job.nant, 2u);
+  dim3 grid(4u * (unsigned)nt, (unsigned)job.nant, 1u);
   kern<<<grid, 512, smem, s>>>(prm);
   return cudaGetLastError();
 }

@@ -15,13 +15,17 @@ namespace gxc {
 constexpr int CW = 16;
 
 // Per-(antenna, FFT) geometry record, produced by the geometry kernel from the
-// delay polynomial (fxkernel/src/fxkernel.cpp:288-309, :425-440).
+// delay polynomial (fxkernel/src/fxkernel.cpp:288-309, :425-440).  The phase
+// constants of the F-stage are evaluated there in FP64, once per (antenna, FFT),
+// reduced mod 1 turn and rounded to FP32 (fxkernel.cpp:503-535, :600-630).
 struct Geom {
-  double a;      // delay gradient across the FFT (s per FFT interval)
-  double b;      // delay at the start of the FFT (s)
-  double frac;   // residual fractional delay (s)
+  float c0;      // fringe phase at the first sample, turns, in [0, 1)
+  float c1;      // fringe phase slope, turns per sample
+  float cstep;   // phase advance of one coarse rotator-table entry, turns
+  float cf;      // fractional-sample correction, turns per channel
   int offset;    // first sample of the FFT window in the antenna stream
   int valid;     // 0 = flagged (window outside the buffer)
+  int pad[2];
 };
 static_assert(sizeof(Geom) == 32, "Geom layout");
 

@@ -743,44 +743,56 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big_kernel(Params p) {
       if (ch >= BIG_STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / BIG_STAGES) - 1) & 1, p.err)) break;
       unsigned char *stage = smem + (size_t)st * BIG_STAGE_BYTES;
       const int tb = ch * KC;
-      for (int task = tid; task < ntask; task += NPROD) {
-        const int s = task % n;
-        const int o = task / n;
-        uint4 re, im;
-        if constexpr (F8) {
-          // 16 E4M3 pairs (re low byte, im high byte) -> 16 re bytes and 16 im bytes
-          uint32_t w[8];
+      // four tasks per thread in flight: all their loads are issued before the first
+      // corner-turn (the loads are 2- or 4-byte gathers, so latency, not bandwidth, rules)
+      constexpr int U = 4;
+      constexpr int NL = F8 ? 16 : 8;  // loads per task
+      for (int task0 = tid; task0 < ntask; task0 += U * NPROD) {
+        uint32_t w[U][NL];
 #pragma unroll
-          for (int i = 0; i < 8; i++) {
-            uint32_t h2[2];
+        for (int u = 0; u < U; u++) {
+          const int task = task0 + u * NPROD;
+          const int s = task % n;
+          const int o = task / n;
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-              const int t = tb + 16 * o + 2 * i + h;
-              h2[h] = (t < p.nt) ? (uint32_t)__ldg(reinterpret_cast<const unsigned short *>(
-                                       src + ((size_t)t * n + s) * CW * esz))
-                                 : 0u;
+          for (int i = 0; i < NL; i++) {
+            const int t = tb + NL * o + i;
+            if (task < ntask && t < p.nt) {
+              const unsigned char *a = src + ((size_t)t * n + s) * CW * esz;
+              w[u][i] = F8 ? (uint32_t)__ldg(reinterpret_cast<const unsigned short *>(a))
+                           : __ldg(reinterpret_cast<const uint32_t *>(a));
+            } else {
+              w[u][i] = 0u;
             }
-            w[i] = h2[0] | (h2[1] << 16);  // re(2i), im(2i), re(2i+1), im(2i+1)
           }
-          re = make_uint4(prmt(w[0], w[1], 0x6420), prmt(w[2], w[3], 0x6420), prmt(w[4], w[5], 0x6420),
-                          prmt(w[6], w[7], 0x6420));
-          im = make_uint4(prmt(w[0], w[1], 0x7531), prmt(w[2], w[3], 0x7531), prmt(w[4], w[5], 0x7531),
-                          prmt(w[6], w[7], 0x7531));
-        } else {
-          uint32_t w[8];
-#pragma unroll
-          for (int i = 0; i < 8; i++) {
-            const int t = tb + 8 * o + i;
-            w[i] = (t < p.nt) ? __ldg(reinterpret_cast<const uint32_t *>(src + ((size_t)t * n + s) * CW * esz)) : 0u;
-          }
-          re = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410), prmt(w[4], w[5], 0x5410),
-                          prmt(w[6], w[7], 0x5410));
-          im = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632), prmt(w[4], w[5], 0x7632),
-                          prmt(w[6], w[7], 0x7632));
         }
-        const int row = 2 * s;
-        *reinterpret_cast<uint4 *>(stage + row * 128 + ((o ^ (row & 7)) << 4)) = re;
-        *reinterpret_cast<uint4 *>(stage + (row + 1) * 128 + ((o ^ ((row + 1) & 7)) << 4)) = im;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int task = task0 + u * NPROD;
+          if (task >= ntask) break;
+          const int s = task % n;
+          const int o = task / n;
+          uint4 re, im;
+          if constexpr (F8) {
+            // 16 E4M3 pairs (re low byte, im high byte) -> 16 re bytes and 16 im bytes
+            uint32_t x[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++) x[i] = w[u][2 * i] | (w[u][2 * i + 1] << 16);  // re, im, re', im'
+            re = make_uint4(prmt(x[0], x[1], 0x6420), prmt(x[2], x[3], 0x6420), prmt(x[4], x[5], 0x6420),
+                            prmt(x[6], x[7], 0x6420));
+            im = make_uint4(prmt(x[0], x[1], 0x7531), prmt(x[2], x[3], 0x7531), prmt(x[4], x[5], 0x7531),
+                            prmt(x[6], x[7], 0x7531));
+          } else {
+            const uint32_t *x = w[u];
+            re = make_uint4(prmt(x[0], x[1], 0x5410), prmt(x[2], x[3], 0x5410), prmt(x[4], x[5], 0x5410),
+                            prmt(x[6], x[7], 0x5410));
+            im = make_uint4(prmt(x[0], x[1], 0x7632), prmt(x[2], x[3], 0x7632), prmt(x[4], x[5], 0x7632),
+                            prmt(x[6], x[7], 0x7632));
+          }
+          const int row = 2 * s;
+          *reinterpret_cast<uint4 *>(stage + row * 128 + ((o ^ (row & 7)) << 4)) = re;
+          *reinterpret_cast<uint4 *>(stage + (row + 1) * 128 + ((o ^ ((row + 1) & 7)) << 4)) = im;
+        }
       }
       fence_proxy_async_smem();
       mbar_arrive(smem_u32(&bar_full[st]));
