@@ -12,14 +12,17 @@
 // padded to a power of two >= 16); four such groups fill the 512 TMEM columns,
 // so a CTA owns CS = 4g channels for the whole FFT block.
 //
-// Roles (288 threads): warps 0-7 load the channelised block from global memory
-// (16-byte loads, [ctile][t][stream][16] half2 layout), corner-turn it in
-// registers into K-contiguous rows and store it swizzled into a 3-stage smem
-// ring; warp 8 allocates TMEM and one lane issues the MMAs and commits to the
-// stage-release barriers; warps 0-3 then read TMEM (tcgen05.ld) and fold the
-// Gram entries into the compensated visibility accumulators.
+// Roles (288 threads): producer thread 0 streams the channelised block
+// ([ctile][t][stream][16] as the F-stage wrote it) into a 3-stage raw ring with
+// TMA tile loads (cp.async.bulk.tensor, completion counted on mbarriers); warps
+// 0-7 corner-turn each raw tile from shared memory into K-contiguous rows and
+// store them swizzled (SW128) into a 2-stage operand ring; warp 8 allocates TMEM
+// and one lane issues the MMAs and commits to the stage-release barriers; warps
+// 0-3 then read TMEM (tcgen05.ld) and fold the Gram entries into the compensated
+// visibility accumulators.  The 33-64 antenna kernel loads with plain gathers.
 // Every mbarrier wait is bounded (iteration cap and %globaltimer); on expiry
 // the kernel raises an error flag, lets issued MMAs drain, frees TMEM and exits.
+#include <cuda.h>
 #include <stdint.h>
 
 #include "gxc_internal.h"
@@ -28,7 +31,11 @@ namespace gxc {
 
 namespace tc {
 
-constexpr int STAGES = 3;
+constexpr int STAGES = 2;                        // operand (SW128) stages
+// Raw ring of the TMA-fed kernels: each stage holds one TMA tile of the channelised
+// block, [t][stream][channels of this CTA] as stored, at most 32 KiB.
+constexpr int RSTAGES = 3;
+constexpr int RAW_BYTES = 32768;
 constexpr int TILE_BYTES = 128 * 128;            // 128 rows x 128 bytes (one SW128 K-major tile)
 constexpr int NPROD_WARPS = 8;
 constexpr int NPROD = NPROD_WARPS * 32;
@@ -161,6 +168,47 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
                : "memory");
 }
 
+// Arrive on the mbarrier and add `bytes` to the transaction count of its current phase.
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// TMA tile load of a 4-D box at element coordinates (x, y, z, w) into shared memory;
+// completion is counted in bytes on the mbarrier.  Boxes reaching past the tensor's
+// extent are filled with zeros.
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int x, int y, int z, int w,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(bar)
+      : "memory");
+}
+
+// Named barrier 1 over the NPROD producer threads with an AND vote: every producer
+// leaves with the same verdict, so a failed wait anywhere ends the loop everywhere.
+__device__ __forceinline__ bool producers_vote(bool ok) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, 1, %2, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)ok), "n"(NPROD)
+      : "memory");
+  return r != 0;
+}
+
+// Wait for a phase with the time limit only (used to let issued copies land before exit).
+__device__ __forceinline__ void mbar_wait_drain(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = globaltimer();
+  for (uint32_t i = 0; i < (1u << 26); i++) {
+    if (mbar_try_wait(bar, parity)) return;
+    if ((i & 255u) == 255u && globaltimer() - t0 > WAIT_NS) return;
+  }
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
   asm volatile(
@@ -204,6 +252,9 @@ struct Params {
   int R, g, CS;         // rows per channel block, channels per MMA group, channels per CTA
   float2 *vsum, *vcomp;
   int *err;
+  // TMA raw tiles (small-N kernels): box = rbx channels x nstream x rkc FFTs, rnbox boxes
+  // (channel tiles) per raw chunk, rbox_bytes each
+  int rbx, rnbox, rkc, rbox_bytes;
 };
 
 // FP16 and FP8 paths: one accumulation over the whole FFT block (its TMEM rounding
@@ -211,13 +262,13 @@ struct Params {
 // A 128-byte SW128 row holds 64 FFTs of FP16 or 128 FFTs of FP8 (E4M3) values;
 // either way one MMA consumes 32 bytes of every row (K = 16 or 32).
 template <bool F8>
-__global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
+__global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p, const __grid_constant__ CUtensorMap tmap) {
   using C = Cfg<false>;
   constexpr int KC = F8 ? 128 : C::KC, KSTEP = F8 ? 32 : C::KSTEP;
   constexpr int NG = C::NG, GROUP_BYTES = C::GROUP_BYTES, STAGE_BYTES = C::STAGE_BYTES;
   constexpr int TMEM_COLS = C::TMEM_COLS;
   extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_done;
+  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], raw_full[RSTAGES], bar_done;
   __shared__ uint32_t tmem_base_sh;
   // 128-byte swizzle atoms need 1024-byte alignment of the shared-window address
   unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -246,6 +297,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
       mbar_init(smem_u32(&bar_full[s]), NPROD);
       mbar_init(smem_u32(&bar_empty[s]), 1);
     }
+    for (int s = 0; s < RSTAGES; s++) mbar_init(smem_u32(&raw_full[s]), 1);
     mbar_init(smem_u32(&bar_done), 1);
     fence_mbar_init();
   }
@@ -261,96 +313,128 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p) {
 
   if (warp < NPROD_WARPS) {
     // ------------------------------------------------------------ producers
+    // Producer thread 0 streams the block through the raw ring with TMA tile loads
+    // (one box per channel tile: [t][stream][rbx channels] as stored, rows past the
+    // block's FFT count zero-filled); all producers corner-turn each raw chunk into
+    // K-contiguous SW128 rows of the operand stage.
+    constexpr int TK = F8 ? 16 : 8;           // FFTs per 16-byte K chunk of a row
+    constexpr int ESZ = F8 ? 2 : 4;           // bytes per complex value
+    const int KCR = p.rkc;                    // FFTs per raw chunk (divides KC)
+    const int RPO = KC / KCR;                 // raw chunks per operand stage
+    const int nraw = nchunks * RPO;
+    const int BX = p.rbx, boxb = p.rbox_bytes;
+    const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(BX - 1)) : 0;
+    const int cofs = p.rnbox == 1 ? (cb & 15) - x0 : 0;  // box index of this CTA's first channel
+    const uint32_t raw_s = sbase + STAGES * STAGE_BYTES;
+    const unsigned char *raw0 = smem + STAGES * STAGE_BYTES;
+    auto issue = [&](int rc) {
+      const int rs = rc % RSTAGES;
+      const uint32_t bar = smem_u32(&raw_full[rs]);
+      mbar_expect_tx(bar, (uint32_t)(boxb * p.rnbox));
+      for (int j = 0; j < p.rnbox; j++)
+        tma_load_4d(raw_s + rs * RAW_BYTES + j * boxb, &tmap, x0, 0, rc * KCR, (cb >> 4) + j, bar);
+    };
+    if (tid == 0)
+      for (int rc = 0; rc < RSTAGES && rc < nraw; rc++) issue(rc);
     const int nq = p.CS / 4;                  // channel quads (CS >= 4)
-    const int ntask = 8 * n * nq;             // (16-byte chunk, stream, channel group) per stage
-    for (int ch = 0; ch < nchunks; ch++) {
+    const int kq = KCR / TK;                  // K chunks per raw chunk
+    const int ntask = kq * n * nq;            // (channel quad, stream, K chunk) per raw chunk
+    const size_t tstride = (size_t)n * BX * ESZ;  // bytes between FFT rows of a box
+    int consumed = 0;
+    bool ok = true;
+    for (int ch = 0; ch < nchunks && ok; ch++) {
       const int st = ch % STAGES;
-      if (ch >= STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err)) break;
+      if (ch >= STAGES) ok = mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err);
       unsigned char *stage = smem + (size_t)st * STAGE_BYTES;
-      const int tb = ch * KC;
-      // task = (channel quad q, stream s, 16-byte K chunk o), q then s fastest across
-      // lanes: a warp's loads of one FFT are contiguous 16-byte pieces (measured faster
-      // here than chunk-fastest lanes, whose conflict-free stores cost extra L1 traffic)
-      for (int task0 = tid; task0 < ntask; task0 += 2 * NPROD) {
+      for (int r = 0; r < RPO; r++) {
+        const int rc = ch * RPO + r;
+        const int rs = rc % RSTAGES;
+        ok = ok && mbar_wait(smem_u32(&raw_full[rs]), (rc / RSTAGES) & 1, p.err);
+        if (ok) {
+          const unsigned char *raw = raw0 + rs * RAW_BYTES;
+          // task = (channel quad q, stream s, K chunk o), q then s fastest across lanes:
+          // a warp reads consecutive 16-byte (or 8-byte) pieces of one FFT row
+          for (int task0 = tid; task0 < ntask; task0 += 2 * NPROD) {
 #pragma unroll
-        for (int u2 = 0; u2 < 2; u2++) {
-          const int task = task0 + u2 * NPROD;
-          if (task >= ntask) break;
-          const int q = task % nq;
-          const int rest = task / nq;
-          const int s = rest % n;
-          const int o = rest / n;
-          if constexpr (F8) {
-            const int c = cb + 4 * q;
-            const int ctile = c >> 4, coff = c & 15;
-            // 16 FFTs x 4 channels of E4M3 pairs (8 bytes per FFT) -> 8 rows (4 channels x re/im)
-            // of 16 FFT bytes: two prmt gather one channel's (re, im) bytes of 2 FFTs each, a
-            // third and fourth split them into 4 re bytes and 4 im bytes
-            const __nv_fp8x2_e4m3 *src =
-                (const __nv_fp8x2_e4m3 *)p.chan + ((size_t)ctile * p.T * n + s) * CW + coff;
-            uint2 v[16];
+            for (int u2 = 0; u2 < 2; u2++) {
+              const int task = task0 + u2 * NPROD;
+              if (task >= ntask) break;
+              const int q = task % nq;
+              const int rest = task / nq;
+              const int s = rest % n;
+              const int o = rest / n;
+              const int oo = r * kq + o;      // K chunk within the 128-byte row
+              const int cc0 = cofs + 4 * q;   // first channel of the quad, counted in the boxes
+              const unsigned char *src =
+                  raw + (cc0 >> 4) * boxb + ((size_t)(o * TK) * n + s) * BX * ESZ + (cc0 & 15) * ESZ;
+              if constexpr (F8) {
+                // 16 FFTs x 4 channels of E4M3 pairs (8 bytes per FFT) -> 8 rows (4 channels x re/im)
+                // of 16 FFT bytes: two prmt gather one channel's (re, im) bytes of 2 FFTs each, a
+                // third and fourth split them into 4 re bytes and 4 im bytes
+                uint2 v[16];
 #pragma unroll
-            for (int i = 0; i < 16; i++) {
-              const int t = tb + 16 * o + i;
-              v[i] = (t < p.nt) ? __ldg(reinterpret_cast<const uint2 *>(src + (size_t)t * n * CW))
-                                : make_uint2(0, 0);
-            }
+                for (int i = 0; i < 16; i++) v[i] = *reinterpret_cast<const uint2 *>(src + i * tstride);
 #pragma unroll
-            for (int ci = 0; ci < 4; ci++) {
-              const int cc = 4 * q + ci;
-              const int G = cc / p.g, gi = cc - G * p.g;
-              const int row = gi * p.R + 2 * s;
-              const uint32_t sel = (ci & 1) ? 0x7362u : 0x5140u;
-              uint32_t re[4], im[4];
+                for (int ci = 0; ci < 4; ci++) {
+                  const int cc = 4 * q + ci;
+                  const int G = cc / p.g, gi = cc - G * p.g;
+                  const int row = gi * p.R + 2 * s;
+                  const uint32_t sel = (ci & 1) ? 0x7362u : 0x5140u;
+                  uint32_t re[4], im[4];
 #pragma unroll
-              for (int k = 0; k < 4; k++) {
-                const uint32_t a0 = (ci < 2) ? v[4 * k].x : v[4 * k].y, a1 = (ci < 2) ? v[4 * k + 1].x : v[4 * k + 1].y;
-                const uint32_t a2 = (ci < 2) ? v[4 * k + 2].x : v[4 * k + 2].y;
-                const uint32_t a3 = (ci < 2) ? v[4 * k + 3].x : v[4 * k + 3].y;
-                const uint32_t t0 = prmt(a0, a1, sel), t1 = prmt(a2, a3, sel);
-                re[k] = prmt(t0, t1, 0x5410);
-                im[k] = prmt(t0, t1, 0x7632);
+                  for (int k = 0; k < 4; k++) {
+                    const uint32_t a0 = (ci < 2) ? v[4 * k].x : v[4 * k].y;
+                    const uint32_t a1 = (ci < 2) ? v[4 * k + 1].x : v[4 * k + 1].y;
+                    const uint32_t a2 = (ci < 2) ? v[4 * k + 2].x : v[4 * k + 2].y;
+                    const uint32_t a3 = (ci < 2) ? v[4 * k + 3].x : v[4 * k + 3].y;
+                    const uint32_t t0 = prmt(a0, a1, sel), t1 = prmt(a2, a3, sel);
+                    re[k] = prmt(t0, t1, 0x5410);
+                    im[k] = prmt(t0, t1, 0x7632);
+                  }
+                  unsigned char *gbase = stage + G * GROUP_BYTES;
+                  *reinterpret_cast<uint4 *>(gbase + row * 128 + ((oo ^ (row & 7)) << 4)) =
+                      make_uint4(re[0], re[1], re[2], re[3]);
+                  *reinterpret_cast<uint4 *>(gbase + (row + 1) * 128 + ((oo ^ ((row + 1) & 7)) << 4)) =
+                      make_uint4(im[0], im[1], im[2], im[3]);
+                }
+              } else {
+                // 8 FFTs x 4 channels of FP16 complex -> 8 rows (4 channels x re/im) of 8 FFTs
+                uint4 v[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) v[i] = *reinterpret_cast<const uint4 *>(src + i * tstride);
+#pragma unroll
+                for (int ci = 0; ci < 4; ci++) {
+                  const int cc = 4 * q + ci;
+                  const int G = cc / p.g, gi = cc - G * p.g;
+                  const int row = gi * p.R + 2 * s;
+                  uint32_t w[8];
+#pragma unroll
+                  for (int i = 0; i < 8; i++)
+                    w[i] = (ci == 0) ? v[i].x : (ci == 1) ? v[i].y : (ci == 2) ? v[i].z : v[i].w;
+                  const uint4 re = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410),
+                                              prmt(w[4], w[5], 0x5410), prmt(w[6], w[7], 0x5410));
+                  const uint4 im = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632),
+                                              prmt(w[4], w[5], 0x7632), prmt(w[6], w[7], 0x7632));
+                  unsigned char *gbase = stage + G * GROUP_BYTES;
+                  *reinterpret_cast<uint4 *>(gbase + row * 128 + ((oo ^ (row & 7)) << 4)) = re;
+                  *reinterpret_cast<uint4 *>(gbase + (row + 1) * 128 + ((oo ^ ((row + 1) & 7)) << 4)) = im;
+                }
               }
-              unsigned char *gbase = stage + G * GROUP_BYTES;
-              *reinterpret_cast<uint4 *>(gbase + row * 128 + ((o ^ (row & 7)) << 4)) =
-                  make_uint4(re[0], re[1], re[2], re[3]);
-              *reinterpret_cast<uint4 *>(gbase + (row + 1) * 128 + ((o ^ ((row + 1) & 7)) << 4)) =
-                  make_uint4(im[0], im[1], im[2], im[3]);
-            }
-          } else {
-            const int c = cb + 4 * q;
-            const int ctile = c >> 4, coff = c & 15;
-            // 8 FFTs x 4 channels of FP16 complex -> 8 rows (4 channels x re/im) of 8 FFTs
-            const __half2 *src = (const __half2 *)p.chan + ((size_t)ctile * p.T * n + s) * CW + coff;
-            uint4 v[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-              const int t = tb + 8 * o + i;
-              v[i] = (t < p.nt) ? __ldg(reinterpret_cast<const uint4 *>(src + (size_t)t * n * CW))
-                                : make_uint4(0, 0, 0, 0);
-            }
-#pragma unroll
-            for (int ci = 0; ci < 4; ci++) {
-              const int cc = 4 * q + ci;
-              const int G = cc / p.g, gi = cc - G * p.g;
-              const int row = gi * p.R + 2 * s;
-              uint32_t w[8];
-#pragma unroll
-              for (int i = 0; i < 8; i++)
-                w[i] = (ci == 0) ? v[i].x : (ci == 1) ? v[i].y : (ci == 2) ? v[i].z : v[i].w;
-              const uint4 re = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410),
-                                          prmt(w[4], w[5], 0x5410), prmt(w[6], w[7], 0x5410));
-              const uint4 im = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632),
-                                          prmt(w[4], w[5], 0x7632), prmt(w[6], w[7], 0x7632));
-              unsigned char *gbase = stage + G * GROUP_BYTES;
-              *reinterpret_cast<uint4 *>(gbase + row * 128 + ((o ^ (row & 7)) << 4)) = re;
-              *reinterpret_cast<uint4 *>(gbase + (row + 1) * 128 + ((o ^ ((row + 1) & 7)) << 4)) = im;
             }
           }
         }
+        ok = producers_vote(ok);  // also: every producer is done reading this raw stage
+        if (!ok) break;
+        consumed = rc + 1;
+        if (tid == 0 && rc + RSTAGES < nraw) issue(rc + RSTAGES);
       }
+      if (!ok) break;
       fence_proxy_async_smem();
       mbar_arrive(smem_u32(&bar_full[st]));
+    }
+    if (!ok && tid == 0) {  // let the copies already issued land before the CTA exits
+      const int issued = consumed + RSTAGES < nraw ? consumed + RSTAGES : nraw;
+      for (int rc = consumed; rc < issued; rc++) mbar_wait_drain(smem_u32(&raw_full[rc % RSTAGES]), (rc / RSTAGES) & 1);
     }
   } else if (lane == 0) {
     // ------------------------------------------------------------ MMA issuer
@@ -444,7 +528,8 @@ constexpr int NEPI_WARPS = 4;
 constexpr int NTHREADS_SPLIT = NPROD + 32 + NEPI_WARPS * 32;
 
 template <int R>
-__global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Params p) {
+__global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Params p,
+                                                                            const __grid_constant__ CUtensorMap tmap) {
   using C = Cfg<true>;
   constexpr int KC = C::KC, NG = C::NG, GROUP_BYTES = C::GROUP_BYTES, STAGE_BYTES = C::STAGE_BYTES;
   constexpr int NSET = 2, SET_COLS = NG * 128, TMEM_COLS = NSET * SET_COLS;  // 512
@@ -454,7 +539,8 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
   constexpr int PP = R / 16;             // pieces in one channel block
   static_assert(TMEM_COLS == 512, "TMEM budget");
   extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_ready[NSET], bar_drained[NSET], bar_done;
+  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], raw_full[RSTAGES], bar_ready[NSET],
+      bar_drained[NSET], bar_done;
   __shared__ uint32_t tmem_base_sh;
   unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   const uint32_t sbase = smem_u32(smem);
@@ -482,6 +568,7 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
       mbar_init(smem_u32(&bar_full[s]), NPROD);
       mbar_init(smem_u32(&bar_empty[s]), 1);
     }
+    for (int s = 0; s < RSTAGES; s++) mbar_init(smem_u32(&raw_full[s]), 1);
     for (int b = 0; b < NSET; b++) {
       mbar_init(smem_u32(&bar_ready[b]), 1);
       mbar_init(smem_u32(&bar_drained[b]), NEPI_WARPS * 32);
@@ -501,42 +588,62 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
 
   if (warp < NPROD_WARPS) {
     // ------------------------------------------------------------ producers
+    // Producer thread 0 streams the block through the raw ring with TMA tile loads
+    // (one raw chunk of KC FFTs per operand stage, rows past the block zero-filled);
+    // all producers split each FP32 value into TF32 hi and lo and store both tiles.
+    const int BX = p.rbx, boxb = p.rbox_bytes;
+    const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(BX - 1)) : 0;
+    const int cofs = p.rnbox == 1 ? (cb & 15) - x0 : 0;
+    const uint32_t raw_s = sbase + STAGES * STAGE_BYTES;
+    const unsigned char *raw0 = smem + STAGES * STAGE_BYTES;
+    auto issue = [&](int rc) {
+      const int rs = rc % RSTAGES;
+      const uint32_t bar = smem_u32(&raw_full[rs]);
+      mbar_expect_tx(bar, (uint32_t)(boxb * p.rnbox));
+      for (int j = 0; j < p.rnbox; j++)
+        tma_load_4d(raw_s + rs * RAW_BYTES + j * boxb, &tmap, x0, 0, rc * KC, (cb >> 4) + j, bar);
+    };
+    if (tid == 0)
+      for (int rc = 0; rc < RSTAGES && rc < nchunks; rc++) issue(rc);
     const int nq = p.CS / 2;        // channel pairs
     const int ntask = 8 * n * nq;   // (16-byte chunk of 4 FFTs, stream, pair) per stage
+    const size_t tstride = (size_t)n * BX * 8;  // bytes between FFT rows of a box
+    int consumed = 0;
+    bool ok = true;
     for (int ch = 0; ch < nchunks; ch++) {
       const int st = ch % STAGES;
-      if (ch >= STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err)) break;
+      const int rs = ch % RSTAGES;
+      if (ch >= STAGES) ok = mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err);
+      ok = ok && mbar_wait(smem_u32(&raw_full[rs]), (ch / RSTAGES) & 1, p.err);
       unsigned char *stage = smem + (size_t)st * STAGE_BYTES;
-      const int tb = ch * KC;
-      // task = (16-byte K chunk o, stream s, channel pair q), o fastest across lanes
-      // (whole swizzled rows per 8 lanes), two tasks' loads in flight per thread
-      for (int task0 = tid; task0 < ntask; task0 += 2 * NPROD) {
+      const unsigned char *raw = raw0 + rs * RAW_BYTES;
+      // task = (pair q, stream s, 16-byte K chunk o), q then s fastest across lanes: a
+      // warp reads consecutive 16-byte pieces of one FFT row (conflict-free), two
+      // tasks per thread in flight
+      for (int task0 = tid; ok && task0 < ntask; task0 += 2 * NPROD) {
         float4 v[2][4];
 #pragma unroll
         for (int u2 = 0; u2 < 2; u2++) {
           const int task = task0 + u2 * NPROD;
-          const int o = task & 7;
-          const int rest = task >> 3;
-          const int q = rest % nq;
-          const int s = rest / nq;
-          const int c2 = cb + 2 * q;
-          const float2 *src = (const float2 *)p.chan + ((size_t)(c2 >> 4) * p.T * n + s) * CW + (c2 & 15);
+          const int q = task % nq;
+          const int rest = task / nq;
+          const int s = rest % n;
+          const int o = rest / n;
+          const int cc0 = cofs + 2 * q;
+          const unsigned char *src = raw + (cc0 >> 4) * boxb + ((size_t)(4 * o) * n + s) * BX * 8 + (cc0 & 15) * 8;
 #pragma unroll
-          for (int i = 0; i < 4; i++) {
-            const int t = tb + 4 * o + i;
-            v[u2][i] = (task < ntask && t < p.nt)
-                           ? __ldg(reinterpret_cast<const float4 *>(src + (size_t)t * n * CW))
-                           : make_float4(0.f, 0.f, 0.f, 0.f);
-          }
+          for (int i = 0; i < 4; i++)
+            v[u2][i] = task < ntask ? *reinterpret_cast<const float4 *>(src + i * tstride)
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
         for (int u2 = 0; u2 < 2; u2++) {
           const int task = task0 + u2 * NPROD;
           if (task >= ntask) break;
-          const int o = task & 7;
-          const int rest = task >> 3;
-          const int q = rest % nq;
-          const int s = rest / nq;
+          const int q = task % nq;
+          const int rest = task / nq;
+          const int s = rest % n;
+          const int o = rest / n;
 #pragma unroll
           for (int ci = 0; ci < 2; ci++) {
             const int cc = 2 * q + ci;
@@ -560,8 +667,16 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
           }
         }
       }
+      ok = producers_vote(ok);  // also: every producer is done reading this raw stage
+      if (!ok) break;
+      consumed = ch + 1;
+      if (tid == 0 && ch + RSTAGES < nchunks) issue(ch + RSTAGES);
       fence_proxy_async_smem();
       mbar_arrive(smem_u32(&bar_full[st]));
+    }
+    if (!ok && tid == 0) {  // let the copies already issued land before the CTA exits
+      const int issued = consumed + RSTAGES < nchunks ? consumed + RSTAGES : nchunks;
+      for (int rc = consumed; rc < issued; rc++) mbar_wait_drain(smem_u32(&raw_full[rc % RSTAGES]), (rc / RSTAGES) & 1);
     }
   } else if (warp == NPROD_WARPS) {
     // ------------------------------------------------------------ MMA issuer
@@ -909,6 +1024,43 @@ cudaError_t xstage_tensor_take_error(int *flag) {
   return e;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link dependency).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(ptr);
+  }
+  return fn;
+}
+
+// Tensor map of the channelised block [ctile][T][n][16] (esz bytes per complex value) for the
+// raw TMA tiles of the small-N tensor kernels: dims (channel in tile, stream, FFT, tile), the
+// FFT extent cut at nt so rows of later FFTs read as zeros; box (bx, n, kc, 1).
+static cudaError_t raw_tensor_map(CUtensorMap *m, const void *chan, int esz, int n, int nt, int T, int nchan, int bx,
+                                  int kc) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return cudaErrorNotSupported;
+  const CUtensorMapDataType dt = esz == 8   ? CU_TENSOR_MAP_DATA_TYPE_INT64
+                                 : esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32
+                                            : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+  const cuuint64_t dims[4] = {(cuuint64_t)CW, (cuuint64_t)n, (cuuint64_t)nt, (cuuint64_t)(nchan / CW)};
+  const cuuint64_t strides[3] = {(cuuint64_t)CW * esz, (cuuint64_t)CW * n * esz, (cuuint64_t)CW * n * T * esz};
+  const cuuint32_t box[4] = {(cuuint32_t)bx, (cuuint32_t)n, (cuuint32_t)kc, 1u};
+  const cuuint32_t estr[4] = {1u, 1u, 1u, 1u};
+  const CUresult r = fn(m, dt, 4, const_cast<void *>(chan), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 // Channels per CTA of the tensor-core X-stage for nant antennas (the channel count must divide by it).
 int xstage_tensor_channels_per_cta(int nant, int chan_type) {
   if (4 * nant > 128) return chan_type == CHAN_F32 ? 0 : 1;  // split-M kernel: one channel, FP16 or FP8
@@ -946,19 +1098,38 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   p.vcomp = vcomp;
   cudaError_t e = xstage_tensor_error_flag(&p.err);
   if (e != cudaSuccess) return e;
-  const size_t smem = (size_t)tc::STAGES * 65536 + 1024;
-  static_assert(tc::Cfg<true>::STAGE_BYTES == 65536 && tc::Cfg<false>::STAGE_BYTES == 65536, "stage size");
   if (R > 128) {
     const size_t bsmem = (size_t)tc::BIG_STAGES * tc::BIG_STAGE_BYTES + 1024;
     auto kern = chan_type == CHAN_F8 ? tc::xstage_tc_big_kernel<true> : tc::xstage_tc_big_kernel<false>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
     if (e != cudaSuccess) return e;
     kern<<<nchan, tc::NTHREADS, bsmem, s>>>(p);
-  } else if (chan_type == CHAN_F32) {
+    return cudaGetLastError();
+  }
+  // small-N kernels: raw TMA tiles of rbx channels (at least 16 bytes: FP8 with 4 channels per
+  // CTA loads 8, of which the CTA uses its 4) x all streams x rkc FFTs, one box per channel tile
+  const int esz = (int)chan_elem_bytes(chan_type);
+  const int KC = chan_type == CHAN_F32 ? tc::Cfg<true>::KC : chan_type == CHAN_F8 ? 128 : tc::Cfg<false>::KC;
+  p.rnbox = p.CS > CW ? p.CS / CW : 1;
+  p.rbx = p.CS > CW ? CW : (p.CS * esz >= 16 ? p.CS : 16 / esz);
+  if (p.rbx * esz < 16 || p.rbx > CW || (p.CS > CW && p.CS % CW)) return cudaErrorInvalidValue;
+  int kc = KC;
+  while (kc > 8 && (size_t)p.rnbox * p.rbx * p.nstream * kc * esz > (size_t)tc::RAW_BYTES) kc >>= 1;
+  p.rkc = kc;
+  p.rbox_bytes = p.rbx * p.nstream * kc * esz;
+  if ((size_t)p.rnbox * p.rbox_bytes > (size_t)tc::RAW_BYTES || KC % kc || (chan_type == CHAN_F32 && kc != KC) ||
+      kc % (chan_type == CHAN_F8 ? 16 : 8))
+    return cudaErrorInvalidValue;
+  CUtensorMap tmap;
+  e = raw_tensor_map(&tmap, chan, esz, p.nstream, nt, T, nchan, p.rbx, kc);
+  if (e != cudaSuccess) return e;
+  const size_t smem = (size_t)tc::STAGES * 65536 + (size_t)tc::RSTAGES * tc::RAW_BYTES + 1024;
+  static_assert(tc::Cfg<true>::STAGE_BYTES == 65536 && tc::Cfg<false>::STAGE_BYTES == 65536, "stage size");
+  if (chan_type == CHAN_F32) {
     auto launch = [&](auto kern) -> cudaError_t {
       cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e2 != cudaSuccess) return e2;
-      kern<<<nchan / p.CS, tc::NTHREADS_SPLIT, smem, s>>>(p);
+      kern<<<nchan / p.CS, tc::NTHREADS_SPLIT, smem, s>>>(p, tmap);
       return cudaSuccess;
     };
     switch (R) {
@@ -973,7 +1144,7 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
     auto kern = chan_type == CHAN_F8 ? tc::xstage_tc_kernel<true> : tc::xstage_tc_kernel<false>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<nchan / p.CS, tc::NTHREADS, smem, s>>>(p);
+    kern<<<nchan / p.CS, tc::NTHREADS, smem, s>>>(p, tmap);
   }
   return cudaGetLastError();
 }
