@@ -39,7 +39,9 @@ constexpr int RAW_BYTES = 32768;
 constexpr int TILE_BYTES = 128 * 128;            // 128 rows x 128 bytes (one SW128 K-major tile)
 constexpr int NPROD_WARPS = 8;
 constexpr int NPROD = NPROD_WARPS * 32;
-constexpr int NTHREADS = NPROD + 32;
+constexpr int NTHREADS = NPROD + 32;             // 33-64 antenna kernel: producers + MMA warp
+constexpr int NTHREADS_TC = NPROD + 64;          // TMA-fed kernel: producers + MMA warp + TMA warp
+constexpr int TMA_WARP = NPROD_WARPS + 1;
 constexpr unsigned long long WAIT_NS = 4000000000ull;  // 4 s
 
 // FP16 path: one FP16 tile per group, K = 64 FFTs per stage, 4 groups (512 TMEM columns).
@@ -185,21 +187,6 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map
       : "memory");
 }
 
-// Named barrier 1 over the NPROD producer threads with an AND vote: every producer
-// leaves with the same verdict, so a failed wait anywhere ends the loop everywhere.
-__device__ __forceinline__ bool producers_vote(bool ok) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\t"
-      "setp.ne.u32 p, %1, 0;\n\t"
-      "bar.red.and.pred q, 1, %2, p;\n\t"
-      "selp.u32 %0, 1, 0, q;\n\t}"
-      : "=r"(r)
-      : "r"((uint32_t)ok), "n"(NPROD)
-      : "memory");
-  return r != 0;
-}
-
 // Wait for a phase with the time limit only (used to let issued copies land before exit).
 __device__ __forceinline__ void mbar_wait_drain(uint32_t bar, uint32_t parity) {
   const uint64_t t0 = globaltimer();
@@ -262,13 +249,14 @@ struct Params {
 // A 128-byte SW128 row holds 64 FFTs of FP16 or 128 FFTs of FP8 (E4M3) values;
 // either way one MMA consumes 32 bytes of every row (K = 16 or 32).
 template <bool F8>
-__global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p, const __grid_constant__ CUtensorMap tmap) {
+__global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, const __grid_constant__ CUtensorMap tmap) {
   using C = Cfg<false>;
   constexpr int KC = F8 ? 128 : C::KC, KSTEP = F8 ? 32 : C::KSTEP;
   constexpr int NG = C::NG, GROUP_BYTES = C::GROUP_BYTES, STAGE_BYTES = C::STAGE_BYTES;
   constexpr int TMEM_COLS = C::TMEM_COLS;
   extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], raw_full[RSTAGES], bar_done;
+  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], raw_full[RSTAGES], raw_empty[RSTAGES],
+      bar_done;
   __shared__ uint32_t tmem_base_sh;
   // 128-byte swizzle atoms need 1024-byte alignment of the shared-window address
   unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -283,7 +271,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p, const 
   if (2 * n < p.R) {
     const int pad = p.R - 2 * n;
     const int per_stage = NG * p.g * pad * 8;  // 16-byte words
-    for (int i = tid; i < STAGES * per_stage; i += NTHREADS) {
+    for (int i = tid; i < STAGES * per_stage; i += NTHREADS_TC) {
       const int st = i / per_stage, r0 = i - st * per_stage;
       const int w = r0 & 7, rr = r0 >> 3;
       const int G = rr / (p.g * pad), rem = rr - G * p.g * pad;
@@ -297,7 +285,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p, const 
       mbar_init(smem_u32(&bar_full[s]), NPROD);
       mbar_init(smem_u32(&bar_empty[s]), 1);
     }
-    for (int s = 0; s < RSTAGES; s++) mbar_init(smem_u32(&raw_full[s]), 1);
+    for (int s = 0; s < RSTAGES; s++) {
+      mbar_init(smem_u32(&raw_full[s]), 1);
+      mbar_init(smem_u32(&raw_empty[s]), NPROD_WARPS);
+    }
     mbar_init(smem_u32(&bar_done), 1);
     fence_mbar_init();
   }
@@ -311,130 +302,139 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p, const 
   tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
 
-  if (warp < NPROD_WARPS) {
+  constexpr int TK = F8 ? 16 : 8;             // FFTs per 16-byte K chunk of a row
+  constexpr int ESZ = F8 ? 2 : 4;             // bytes per complex value
+  const int KCR = p.rkc;                      // FFTs per raw chunk (divides KC)
+  const int RPO = KC / KCR;                   // raw chunks per operand stage
+  const int nraw = nchunks * RPO;
+  if (warp == TMA_WARP) {
+    // ------------------------------------------------------------ TMA producer
+    // One lane streams the block through the raw ring: one box per channel tile,
+    // [t][stream][rbx channels] as stored, rows past the block's FFT count zero-filled.
+    if (lane == 0) {
+      const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(p.rbx - 1)) : 0;
+      const uint32_t raw_s = sbase + STAGES * STAGE_BYTES;
+      int issued = 0;
+      for (int rc = 0; rc < nraw; rc++) {
+        const int rs = rc % RSTAGES;
+        if (rc >= RSTAGES && !mbar_wait(smem_u32(&raw_empty[rs]), ((rc / RSTAGES) - 1) & 1, p.err)) break;
+        const uint32_t bar = smem_u32(&raw_full[rs]);
+        mbar_expect_tx(bar, (uint32_t)(p.rbox_bytes * p.rnbox));
+        for (int j = 0; j < p.rnbox; j++)
+          tma_load_4d(raw_s + rs * RAW_BYTES + j * p.rbox_bytes, &tmap, x0, 0, rc * KCR, (cb >> 4) + j, bar);
+        issued = rc + 1;
+      }
+      // every copy issued lands before the CTA can exit (the last RSTAGES are the only
+      // ones possibly unconsumed, and no later phase of their stages was started)
+      for (int rc = issued > RSTAGES ? issued - RSTAGES : 0; rc < issued; rc++)
+        mbar_wait_drain(smem_u32(&raw_full[rc % RSTAGES]), (rc / RSTAGES) & 1);
+    }
+  } else if (warp < NPROD_WARPS) {
     // ------------------------------------------------------------ producers
-    // Producer thread 0 streams the block through the raw ring with TMA tile loads
-    // (one box per channel tile: [t][stream][rbx channels] as stored, rows past the
-    // block's FFT count zero-filled); all producers corner-turn each raw chunk into
-    // K-contiguous SW128 rows of the operand stage.
-    constexpr int TK = F8 ? 16 : 8;           // FFTs per 16-byte K chunk of a row
-    constexpr int ESZ = F8 ? 2 : 4;           // bytes per complex value
-    const int KCR = p.rkc;                    // FFTs per raw chunk (divides KC)
-    const int RPO = KC / KCR;                 // raw chunks per operand stage
-    const int nraw = nchunks * RPO;
+    // Corner-turn each raw chunk into K-contiguous SW128 rows of the operand stage;
+    // every warp releases the raw stage on its own (raw_empty counts warps).
     const int BX = p.rbx, boxb = p.rbox_bytes;
     const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(BX - 1)) : 0;
     const int cofs = p.rnbox == 1 ? (cb & 15) - x0 : 0;  // box index of this CTA's first channel
-    const uint32_t raw_s = sbase + STAGES * STAGE_BYTES;
     const unsigned char *raw0 = smem + STAGES * STAGE_BYTES;
-    auto issue = [&](int rc) {
-      const int rs = rc % RSTAGES;
-      const uint32_t bar = smem_u32(&raw_full[rs]);
-      mbar_expect_tx(bar, (uint32_t)(boxb * p.rnbox));
-      for (int j = 0; j < p.rnbox; j++)
-        tma_load_4d(raw_s + rs * RAW_BYTES + j * boxb, &tmap, x0, 0, rc * KCR, (cb >> 4) + j, bar);
-    };
-    if (tid == 0)
-      for (int rc = 0; rc < RSTAGES && rc < nraw; rc++) issue(rc);
     const int nq = p.CS / 4;                  // channel quads (CS >= 4)
     const int kq = KCR / TK;                  // K chunks per raw chunk
     const int ntask = kq * n * nq;            // (channel quad, stream, K chunk) per raw chunk
     const size_t tstride = (size_t)n * BX * ESZ;  // bytes between FFT rows of a box
-    int consumed = 0;
     bool ok = true;
     for (int ch = 0; ch < nchunks && ok; ch++) {
       const int st = ch % STAGES;
-      if (ch >= STAGES) ok = mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err);
+      if (ch >= STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err)) break;
       unsigned char *stage = smem + (size_t)st * STAGE_BYTES;
       for (int r = 0; r < RPO; r++) {
         const int rc = ch * RPO + r;
         const int rs = rc % RSTAGES;
-        ok = ok && mbar_wait(smem_u32(&raw_full[rs]), (rc / RSTAGES) & 1, p.err);
-        if (ok) {
-          const unsigned char *raw = raw0 + rs * RAW_BYTES;
-          // task = (channel quad q, stream s, K chunk o), q then s fastest across lanes:
-          // a warp reads consecutive 16-byte (or 8-byte) pieces of one FFT row
-          for (int task0 = tid; task0 < ntask; task0 += 2 * NPROD) {
+        if (!mbar_wait(smem_u32(&raw_full[rs]), (rc / RSTAGES) & 1, p.err)) {
+          ok = false;
+          break;
+        }
+        const unsigned char *raw = raw0 + rs * RAW_BYTES;
+        // task = (channel quad q, stream s, K chunk o), q then s fastest across lanes:
+        // a warp reads consecutive 16-byte (or 8-byte) pieces of one FFT row
+        for (int task0 = tid; task0 < ntask; task0 += 2 * NPROD) {
 #pragma unroll
-            for (int u2 = 0; u2 < 2; u2++) {
-              const int task = task0 + u2 * NPROD;
-              if (task >= ntask) break;
-              const int q = task % nq;
-              const int rest = task / nq;
-              const int s = rest % n;
-              const int o = rest / n;
-              const int oo = r * kq + o;      // K chunk within the 128-byte row
-              const int cc0 = cofs + 4 * q;   // first channel of the quad, counted in the boxes
-              const unsigned char *src =
-                  raw + (cc0 >> 4) * boxb + ((size_t)(o * TK) * n + s) * BX * ESZ + (cc0 & 15) * ESZ;
-              if constexpr (F8) {
-                // 16 FFTs x 4 channels of E4M3 pairs (8 bytes per FFT) -> 8 rows (4 channels x re/im)
-                // of 16 FFT bytes: two prmt gather one channel's (re, im) bytes of 2 FFTs each, a
-                // third and fourth split them into 4 re bytes and 4 im bytes
-                uint2 v[16];
+          for (int u2 = 0; u2 < 2; u2++) {
+            const int task = task0 + u2 * NPROD;
+            if (task >= ntask) break;
+            const int q = task % nq;
+            const int rest = task / nq;
+            const int s = rest % n;
+            const int o = rest / n;
+            const int oo = r * kq + o;      // K chunk within the 128-byte row
+            const int cc0 = cofs + 4 * q;   // first channel of the quad, counted in the boxes
+            // which of the pair (re row, im row) this lane stores first: among 8 lanes the
+            // first stores then cover all 8 swizzle positions (no bank conflicts)
+            const int sw = nq == 1 ? ((s >> 2) & 1) : (q & 1);
+            const unsigned char *src =
+                raw + (cc0 >> 4) * boxb + ((size_t)(o * TK) * n + s) * BX * ESZ + (cc0 & 15) * ESZ;
+            if constexpr (F8) {
+              // 16 FFTs x 4 channels of E4M3 pairs (8 bytes per FFT) -> 8 rows (4 channels x re/im)
+              // of 16 FFT bytes: two prmt gather one channel's (re, im) bytes of 2 FFTs each, a
+              // third and fourth split them into 4 re bytes and 4 im bytes
+              uint2 v[16];
 #pragma unroll
-                for (int i = 0; i < 16; i++) v[i] = *reinterpret_cast<const uint2 *>(src + i * tstride);
+              for (int i = 0; i < 16; i++) v[i] = *reinterpret_cast<const uint2 *>(src + i * tstride);
 #pragma unroll
-                for (int ci = 0; ci < 4; ci++) {
-                  const int cc = 4 * q + ci;
-                  const int G = cc / p.g, gi = cc - G * p.g;
-                  const int row = gi * p.R + 2 * s;
-                  const uint32_t sel = (ci & 1) ? 0x7362u : 0x5140u;
-                  uint32_t re[4], im[4];
+              for (int ci = 0; ci < 4; ci++) {
+                const int cc = 4 * q + ci;
+                const int G = cc / p.g, gi = cc - G * p.g;
+                const int row = gi * p.R + 2 * s;
+                const uint32_t sel = (ci & 1) ? 0x7362u : 0x5140u;
+                uint32_t re[4], im[4];
 #pragma unroll
-                  for (int k = 0; k < 4; k++) {
-                    const uint32_t a0 = (ci < 2) ? v[4 * k].x : v[4 * k].y;
-                    const uint32_t a1 = (ci < 2) ? v[4 * k + 1].x : v[4 * k + 1].y;
-                    const uint32_t a2 = (ci < 2) ? v[4 * k + 2].x : v[4 * k + 2].y;
-                    const uint32_t a3 = (ci < 2) ? v[4 * k + 3].x : v[4 * k + 3].y;
-                    const uint32_t t0 = prmt(a0, a1, sel), t1 = prmt(a2, a3, sel);
-                    re[k] = prmt(t0, t1, 0x5410);
-                    im[k] = prmt(t0, t1, 0x7632);
-                  }
-                  unsigned char *gbase = stage + G * GROUP_BYTES;
-                  *reinterpret_cast<uint4 *>(gbase + row * 128 + ((oo ^ (row & 7)) << 4)) =
-                      make_uint4(re[0], re[1], re[2], re[3]);
-                  *reinterpret_cast<uint4 *>(gbase + (row + 1) * 128 + ((oo ^ ((row + 1) & 7)) << 4)) =
-                      make_uint4(im[0], im[1], im[2], im[3]);
+                for (int k = 0; k < 4; k++) {
+                  const uint32_t a0 = (ci < 2) ? v[4 * k].x : v[4 * k].y;
+                  const uint32_t a1 = (ci < 2) ? v[4 * k + 1].x : v[4 * k + 1].y;
+                  const uint32_t a2 = (ci < 2) ? v[4 * k + 2].x : v[4 * k + 2].y;
+                  const uint32_t a3 = (ci < 2) ? v[4 * k + 3].x : v[4 * k + 3].y;
+                  const uint32_t t0 = prmt(a0, a1, sel), t1 = prmt(a2, a3, sel);
+                  re[k] = prmt(t0, t1, 0x5410);
+                  im[k] = prmt(t0, t1, 0x7632);
                 }
-              } else {
-                // 8 FFTs x 4 channels of FP16 complex -> 8 rows (4 channels x re/im) of 8 FFTs
-                uint4 v[8];
+                const uint4 vre = make_uint4(re[0], re[1], re[2], re[3]);
+                const uint4 vim = make_uint4(im[0], im[1], im[2], im[3]);
+                const int ra = row + sw, rb = row + 1 - sw;
+                unsigned char *gbase = stage + G * GROUP_BYTES;
+                *reinterpret_cast<uint4 *>(gbase + ra * 128 + ((oo ^ (ra & 7)) << 4)) = sw ? vim : vre;
+                *reinterpret_cast<uint4 *>(gbase + rb * 128 + ((oo ^ (rb & 7)) << 4)) = sw ? vre : vim;
+              }
+            } else {
+              // 8 FFTs x 4 channels of FP16 complex -> 8 rows (4 channels x re/im) of 8 FFTs
+              uint4 v[8];
 #pragma unroll
-                for (int i = 0; i < 8; i++) v[i] = *reinterpret_cast<const uint4 *>(src + i * tstride);
+              for (int i = 0; i < 8; i++) v[i] = *reinterpret_cast<const uint4 *>(src + i * tstride);
 #pragma unroll
-                for (int ci = 0; ci < 4; ci++) {
-                  const int cc = 4 * q + ci;
-                  const int G = cc / p.g, gi = cc - G * p.g;
-                  const int row = gi * p.R + 2 * s;
-                  uint32_t w[8];
+              for (int ci = 0; ci < 4; ci++) {
+                const int cc = 4 * q + ci;
+                const int G = cc / p.g, gi = cc - G * p.g;
+                const int row = gi * p.R + 2 * s;
+                uint32_t w[8];
 #pragma unroll
-                  for (int i = 0; i < 8; i++)
-                    w[i] = (ci == 0) ? v[i].x : (ci == 1) ? v[i].y : (ci == 2) ? v[i].z : v[i].w;
-                  const uint4 re = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410),
-                                              prmt(w[4], w[5], 0x5410), prmt(w[6], w[7], 0x5410));
-                  const uint4 im = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632),
-                                              prmt(w[4], w[5], 0x7632), prmt(w[6], w[7], 0x7632));
-                  unsigned char *gbase = stage + G * GROUP_BYTES;
-                  *reinterpret_cast<uint4 *>(gbase + row * 128 + ((oo ^ (row & 7)) << 4)) = re;
-                  *reinterpret_cast<uint4 *>(gbase + (row + 1) * 128 + ((oo ^ ((row + 1) & 7)) << 4)) = im;
-                }
+                for (int i = 0; i < 8; i++)
+                  w[i] = (ci == 0) ? v[i].x : (ci == 1) ? v[i].y : (ci == 2) ? v[i].z : v[i].w;
+                const uint4 vre = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410),
+                                             prmt(w[4], w[5], 0x5410), prmt(w[6], w[7], 0x5410));
+                const uint4 vim = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632),
+                                             prmt(w[4], w[5], 0x7632), prmt(w[6], w[7], 0x7632));
+                const int ra = row + sw, rb = row + 1 - sw;
+                unsigned char *gbase = stage + G * GROUP_BYTES;
+                *reinterpret_cast<uint4 *>(gbase + ra * 128 + ((oo ^ (ra & 7)) << 4)) = sw ? vim : vre;
+                *reinterpret_cast<uint4 *>(gbase + rb * 128 + ((oo ^ (rb & 7)) << 4)) = sw ? vre : vim;
               }
             }
           }
         }
-        ok = producers_vote(ok);  // also: every producer is done reading this raw stage
-        if (!ok) break;
-        consumed = rc + 1;
-        if (tid == 0 && rc + RSTAGES < nraw) issue(rc + RSTAGES);
+        __syncwarp();  // this warp's reads of the raw stage are done (their values are stored)
+        if (lane == 0) mbar_arrive(smem_u32(&raw_empty[rs]));
       }
       if (!ok) break;
       fence_proxy_async_smem();
       mbar_arrive(smem_u32(&bar_full[st]));
-    }
-    if (!ok && tid == 0) {  // let the copies already issued land before the CTA exits
-      const int issued = consumed + RSTAGES < nraw ? consumed + RSTAGES : nraw;
-      for (int rc = consumed; rc < issued; rc++) mbar_wait_drain(smem_u32(&raw_full[rc % RSTAGES]), (rc / RSTAGES) & 1);
     }
   } else if (lane == 0) {
     // ------------------------------------------------------------ MMA issuer
@@ -525,7 +525,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_kernel(Params p, const 
 // R (rows per channel block) is a template parameter so the register sums are
 // indexed at compile time.
 constexpr int NEPI_WARPS = 4;
-constexpr int NTHREADS_SPLIT = NPROD + 32 + NEPI_WARPS * 32;
+constexpr int NTHREADS_SPLIT = NPROD + 32 + NEPI_WARPS * 32 + 32;  // + TMA warp (the last)
+constexpr int TMA_WARP_SPLIT = NPROD_WARPS + 1 + NEPI_WARPS;
 
 template <int R>
 __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Params p,
@@ -539,8 +540,8 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
   constexpr int PP = R / 16;             // pieces in one channel block
   static_assert(TMEM_COLS == 512, "TMEM budget");
   extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], raw_full[RSTAGES], bar_ready[NSET],
-      bar_drained[NSET], bar_done;
+  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], raw_full[RSTAGES], raw_empty[RSTAGES],
+      bar_ready[NSET], bar_drained[NSET], bar_done;
   __shared__ uint32_t tmem_base_sh;
   unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   const uint32_t sbase = smem_u32(smem);
@@ -568,7 +569,10 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
       mbar_init(smem_u32(&bar_full[s]), NPROD);
       mbar_init(smem_u32(&bar_empty[s]), 1);
     }
-    for (int s = 0; s < RSTAGES; s++) mbar_init(smem_u32(&raw_full[s]), 1);
+    for (int s = 0; s < RSTAGES; s++) {
+      mbar_init(smem_u32(&raw_full[s]), 1);
+      mbar_init(smem_u32(&raw_empty[s]), NPROD_WARPS);
+    }
     for (int b = 0; b < NSET; b++) {
       mbar_init(smem_u32(&bar_ready[b]), 1);
       mbar_init(smem_u32(&bar_drained[b]), NEPI_WARPS * 32);
@@ -586,41 +590,48 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
   tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
 
-  if (warp < NPROD_WARPS) {
+  if (warp == TMA_WARP_SPLIT) {
+    // ------------------------------------------------------------ TMA producer
+    // One lane streams the block through the raw ring (one raw chunk of KC FFTs per
+    // operand stage, one box per channel tile, rows past the block zero-filled).
+    if (lane == 0) {
+      const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(p.rbx - 1)) : 0;
+      const uint32_t raw_s = sbase + STAGES * STAGE_BYTES;
+      int issued = 0;
+      for (int rc = 0; rc < nchunks; rc++) {
+        const int rs = rc % RSTAGES;
+        if (rc >= RSTAGES && !mbar_wait(smem_u32(&raw_empty[rs]), ((rc / RSTAGES) - 1) & 1, p.err)) break;
+        const uint32_t bar = smem_u32(&raw_full[rs]);
+        mbar_expect_tx(bar, (uint32_t)(p.rbox_bytes * p.rnbox));
+        for (int j = 0; j < p.rnbox; j++)
+          tma_load_4d(raw_s + rs * RAW_BYTES + j * p.rbox_bytes, &tmap, x0, 0, rc * KC, (cb >> 4) + j, bar);
+        issued = rc + 1;
+      }
+      for (int rc = issued > RSTAGES ? issued - RSTAGES : 0; rc < issued; rc++)
+        mbar_wait_drain(smem_u32(&raw_full[rc % RSTAGES]), (rc / RSTAGES) & 1);
+    }
+  } else if (warp < NPROD_WARPS) {
     // ------------------------------------------------------------ producers
-    // Producer thread 0 streams the block through the raw ring with TMA tile loads
-    // (one raw chunk of KC FFTs per operand stage, rows past the block zero-filled);
-    // all producers split each FP32 value into TF32 hi and lo and store both tiles.
+    // Split each FP32 value of a raw chunk into TF32 hi and lo and store both tiles;
+    // every warp releases the raw stage on its own (raw_empty counts warps).
     const int BX = p.rbx, boxb = p.rbox_bytes;
     const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(BX - 1)) : 0;
     const int cofs = p.rnbox == 1 ? (cb & 15) - x0 : 0;
-    const uint32_t raw_s = sbase + STAGES * STAGE_BYTES;
     const unsigned char *raw0 = smem + STAGES * STAGE_BYTES;
-    auto issue = [&](int rc) {
-      const int rs = rc % RSTAGES;
-      const uint32_t bar = smem_u32(&raw_full[rs]);
-      mbar_expect_tx(bar, (uint32_t)(boxb * p.rnbox));
-      for (int j = 0; j < p.rnbox; j++)
-        tma_load_4d(raw_s + rs * RAW_BYTES + j * boxb, &tmap, x0, 0, rc * KC, (cb >> 4) + j, bar);
-    };
-    if (tid == 0)
-      for (int rc = 0; rc < RSTAGES && rc < nchunks; rc++) issue(rc);
     const int nq = p.CS / 2;        // channel pairs
     const int ntask = 8 * n * nq;   // (16-byte chunk of 4 FFTs, stream, pair) per stage
     const size_t tstride = (size_t)n * BX * 8;  // bytes between FFT rows of a box
-    int consumed = 0;
-    bool ok = true;
     for (int ch = 0; ch < nchunks; ch++) {
       const int st = ch % STAGES;
       const int rs = ch % RSTAGES;
-      if (ch >= STAGES) ok = mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err);
-      ok = ok && mbar_wait(smem_u32(&raw_full[rs]), (ch / RSTAGES) & 1, p.err);
+      if (ch >= STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err)) break;
+      if (!mbar_wait(smem_u32(&raw_full[rs]), (ch / RSTAGES) & 1, p.err)) break;
       unsigned char *stage = smem + (size_t)st * STAGE_BYTES;
       const unsigned char *raw = raw0 + rs * RAW_BYTES;
       // task = (pair q, stream s, 16-byte K chunk o), q then s fastest across lanes: a
       // warp reads consecutive 16-byte pieces of one FFT row (conflict-free), two
       // tasks per thread in flight
-      for (int task0 = tid; ok && task0 < ntask; task0 += 2 * NPROD) {
+      for (int task0 = tid; task0 < ntask; task0 += 2 * NPROD) {
         float4 v[2][4];
 #pragma unroll
         for (int u2 = 0; u2 < 2; u2++) {
@@ -644,12 +655,16 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
           const int rest = task / nq;
           const int s = rest % n;
           const int o = rest / n;
+          // which part (re, im) this lane stores first: among 8 lanes the first stores
+          // then cover all 8 swizzle positions (no bank conflicts)
+          const int sw = nq == 1 ? ((s >> 2) & 1) : (q & 1);
 #pragma unroll
           for (int ci = 0; ci < 2; ci++) {
             const int cc = 2 * q + ci;
             const int G = cc / GCH, gi = cc - G * GCH;
 #pragma unroll
-            for (int part = 0; part < 2; part++) {
+            for (int pp = 0; pp < 2; pp++) {
+              const int part = pp ^ sw;
               const int row = gi * R + 2 * s + part;
               uint32_t hi[4], lo[4];
 #pragma unroll
@@ -660,23 +675,17 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
                 lo[i] = __float_as_uint(x - __uint_as_float(hi[i]));
               }
               unsigned char *gbase = stage + G * GROUP_BYTES;
-              const int sw = (o ^ (row & 7)) << 4;
-              *reinterpret_cast<uint4 *>(gbase + row * 128 + sw) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-              *reinterpret_cast<uint4 *>(gbase + TILE_BYTES + row * 128 + sw) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+              const int swz = (o ^ (row & 7)) << 4;
+              *reinterpret_cast<uint4 *>(gbase + row * 128 + swz) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+              *reinterpret_cast<uint4 *>(gbase + TILE_BYTES + row * 128 + swz) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
             }
           }
         }
       }
-      ok = producers_vote(ok);  // also: every producer is done reading this raw stage
-      if (!ok) break;
-      consumed = ch + 1;
-      if (tid == 0 && ch + RSTAGES < nchunks) issue(ch + RSTAGES);
+      __syncwarp();  // this warp's reads of the raw stage are done (their values are stored)
+      if (lane == 0) mbar_arrive(smem_u32(&raw_empty[rs]));
       fence_proxy_async_smem();
       mbar_arrive(smem_u32(&bar_full[st]));
-    }
-    if (!ok && tid == 0) {  // let the copies already issued land before the CTA exits
-      const int issued = consumed + RSTAGES < nchunks ? consumed + RSTAGES : nchunks;
-      for (int rc = consumed; rc < issued; rc++) mbar_wait_drain(smem_u32(&raw_full[rc % RSTAGES]), (rc / RSTAGES) & 1);
     }
   } else if (warp == NPROD_WARPS) {
     // ------------------------------------------------------------ MMA issuer
@@ -1144,7 +1153,7 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
     auto kern = chan_type == CHAN_F8 ? tc::xstage_tc_kernel<true> : tc::xstage_tc_kernel<false>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<nchan / p.CS, tc::NTHREADS, smem, s>>>(p, tmap);
+    kern<<<nchan / p.CS, tc::NTHREADS_TC, smem, s>>>(p, tmap);
   }
   return cudaGetLastError();
 }
