@@ -543,7 +543,12 @@ static cudaError_t launch_fstage_t(const FParams &prm, int nt, cudaStream_t s) {
 constexpr int F15 = 32768;
 constexpr int F15_STRIDE = 128;                 // fringe/frac table split (2^floor(log2 nchan / 2))
 constexpr int F15_SUB = F15 / F15_STRIDE;       // 256
-constexpr int F15_BUF = 64 * 272;               // complex slots: max(128x129, 128x132, 64x272)
+// complex slots of the shared buffer, reused by the passes: [n2][n1] columns 128 x 129,
+// [k1][n2] rows 128 x 132, [k1][k2] rows 64 x 280.  Passes C and D give each row 8 lanes
+// (8 consecutive elements) and 4 rows per warp; a row stride of 280 complex (16 banks mod 32)
+// puts rows 0/2 and 1/3 in opposite bank halves, the minimum of 2 wavefronts per access.
+constexpr int F15_RS = 280;
+constexpr int F15_BUF = 64 * F15_RS;
 // staged rows: 128 samples of one row n1 (4 bytes each for 8-bit complex, 2 bits per
 // pol for 2-bit real) plus the 16-byte rounding of the row start
 template <bool CPLX> struct F15Stage {
@@ -704,7 +709,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_clust
   for (int q = 0; q < 2; q++) {
     const int ivc = t8 + 8 * q;
 #pragma unroll
-    for (int r = 0; r < 16; r++) buf[kr * 272 + ivc * 17 + r] = u[16 * q + r];
+    for (int r = 0; r < 16; r++) buf[kr * F15_RS + ivc * 17 + r] = u[16 * q + r];
   }
   __syncthreads();
   // ---- step 3, pass D: radix 16 (span 16); X[k1 + 128 k2], k2 = ivd + 16 r
@@ -714,7 +719,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_clust
     const int ivd = t8 + 8 * q;
     float2 *v = &u[16 * q];
 #pragma unroll
-    for (int r = 0; r < 16; r++) v[r] = buf[kr * 272 + ivd + 17 * r];
+    for (int r = 0; r < 16; r++) v[r] = buf[kr * F15_RS + ivd + 17 * r];
 #pragma unroll
     for (int r = 1; r < 16; r++) v[r] = cmul(v[r], thi[r * ivd]);  // W_N^(128 r ivd)
     dft<16>(v);
