@@ -8,6 +8,7 @@
 #include <cooperative_groups.h>
 #include <math.h>
 #include <stdlib.h>
+#include <type_traits>
 #include <vector>
 
 #include "gxc_internal.h"
@@ -749,6 +750,175 @@ static cudaError_t launch_fstage_cluster(const FParams &prm, int nt, cudaStream_
   return cudaGetLastError();
 }
 
+// ---------------------------------- 32768-point windows, FP16 / FP8 channelised output
+// One CTA per (pol, FFT), 512 threads, three radix-32 passes over n = iv + 1024 r; each
+// thread owns two 32-point groups (iv = tid, tid + 512) per pass.  The intermediate
+// spectrum lives in shared memory as FP16 (135 KB instead of 256 KB in FP32, so no
+// cluster is needed), scaled by 2^-5 after each of the first two passes: for any input
+// (|x| <= 127*sqrt(2)) the stored values stay below 6000, far inside FP16's range, and the
+// two extra roundings (2^-11 relative) sit below the FP16 / FP8 output rounding.  The
+// scale is undone exactly in the final cast.  In the in-place middle pass every thread
+// keeps its first group's results as half2 registers until the barrier that ends all reads.
+template <typename OutT, bool CPLX>
+__global__ void __launch_bounds__(512, 1) fstage15h_kernel(FParams prm) {
+  constexpr int N = F15, R = 32, NB = N / R, PADN = N + N / R;
+  constexpr int NCHAN = CPLX ? N : N / 2;
+  constexpr int STRIDE = F15_STRIDE, SUB = F15_SUB, FSUB = NCHAN / STRIDE;
+  constexpr float SC = 1.0f / 32.0f;
+  const Job &job = prm.job;
+  extern __shared__ float2 smem[];
+  float2 *tsub = smem;                 // [SUB]
+  float2 *tstep = tsub + SUB;          // [STRIDE]
+  float2 *fsubt = tstep + STRIDE;      // [FSUB]
+  float2 *fstept = fsubt + FSUB;       // [STRIDE]
+  __half2 *buf = reinterpret_cast<__half2 *>(fstept + STRIDE);          // [PADN]
+  unsigned char *stage = reinterpret_cast<unsigned char *>(buf + PADN);  // 2-bit windows only
+
+  const int s = blockIdx.x;  // grid x = stream (pol + 2 * antenna), y = FFT
+  const int pol = s & 1;
+  const int ant = s >> 1;
+  const int tl = blockIdx.y;
+  const int t = prm.t0 + tl;
+  const int tid = threadIdx.x;
+  const int nstreams = 2 * job.nant;
+  OutT *chan = reinterpret_cast<OutT *>(prm.chan);
+  const Geom g = job.geom[(size_t)ant * job.nfft + t];
+  OutT *out0 = chan + ((size_t)tl * nstreams + s) * CW;
+  const size_t ctile_stride = (size_t)prm.T * nstreams * CW;
+  if (!g.valid) {
+    const OutT z = to_out<OutT>(make_float2(0.f, 0.f), 1.f);
+    for (int c = tid; c < NCHAN; c += 512) out0[(size_t)(c >> 4) * ctile_stride + (c & 15)] = z;
+    return;
+  }
+  const long long off = g.offset;
+  long long stage_base = 0;
+  if constexpr (!CPLX) {
+    // 2-bit: stage the packed window with 16-byte loads (the buffer holds (nfft+1)*F samples
+    // and offset <= (nfft-1)*F, so the window plus the 16-byte rounding stays inside it)
+    stage_base = (off >> 1) & ~15LL;
+    const uint4 *src = reinterpret_cast<const uint4 *>(job.inputs[ant] + stage_base);
+    const long long last = (off + N + 1) >> 1;
+    const int nvec = (int)((last - stage_base + 15) >> 4);
+    uint4 *dst = reinterpret_cast<uint4 *>(stage);
+    for (int i = tid; i < nvec; i += 512) dst[i] = __ldg(&src[i]);
+  }
+  for (int k = tid; k < SUB; k += 512) {
+    float sn, cs;
+    sincospif(-2.0f * fmaf((float)k, g.c1, g.c0), &sn, &cs);
+    tsub[k] = make_float2(cs, sn);
+  }
+  for (int i = tid; i < STRIDE; i += 512) {
+    float sn, cs;
+    sincospif(-2.0f * ((float)i * g.cstep), &sn, &cs);
+    tstep[i] = make_float2(cs, sn);
+    sincospif(2.0f * ((float)(i * FSUB) * g.cf), &sn, &cs);
+    fstept[i] = make_float2(cs, sn);
+  }
+  for (int k = tid; k < FSUB; k += 512) {
+    float sn, cs;
+    sincospif(2.0f * ((float)k * g.cf), &sn, &cs);
+    fsubt[k] = make_float2(cs, sn);
+  }
+  __syncthreads();
+
+  // ---- pass 0 (span 1): decode + fringe-rotate, radix 32 over n = iv + NB r
+#pragma unroll 1
+  for (int q = 0; q < 2; q++) {
+    const int iv = tid + 512 * q;
+    float2 u[32];
+    const float2 rs = tsub[iv & (SUB - 1)];  // n mod SUB = iv mod SUB
+    if constexpr (CPLX) {
+      const uint8_t *in = job.inputs[ant] + 4 * (off + iv) + 2 * pol;
+#pragma unroll
+      for (int r = 0; r < 32; r++) {
+        const char2 x = __ldg(reinterpret_cast<const char2 *>(in + 4LL * NB * r));
+        u[r] = cmul(make_float2((float)x.x, (float)x.y), cmul(rs, tstep[(iv / SUB) + r * (NB / SUB)]));
+      }
+    } else {
+      const int sbase = (int)((off >> 1) - stage_base);
+      const int p0 = (int)(off & 1) + iv;
+      const int shift = 2 * (2 * (p0 & 1) + pol);
+#pragma unroll
+      for (int r = 0; r < 32; r++) {
+        const float2 rot = cmul(rs, tstep[(iv / SUB) + r * (NB / SUB)]);
+        const int byte = stage[sbase + (p0 >> 1) + r * (NB / 2)];
+        const float lv = level2bit((byte >> shift) & 3);
+        u[r] = make_float2(lv * rot.x, lv * rot.y);
+      }
+    }
+    dft<32>(u);
+    __half2 *b = buf + iv * (R + 1);
+#pragma unroll
+    for (int r = 0; r < 32; r++) b[r] = __floats2half2_rn(u[r].x * SC, u[r].y * SC);
+  }
+  __syncthreads();
+  // ---- pass 1: radix 32, span 32 (in place: both groups read before any write)
+  {
+    __half2 h[2][32];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const int iv = tid + 512 * q;
+      float2 u[32];
+      const __half2 *b = buf + iv + iv / R;
+#pragma unroll
+      for (int r = 0; r < 32; r++) u[r] = __half22float2(b[r * (NB + NB / R)]);
+      twiddle<N, R, R>(u, iv & (R - 1), prm.tw);
+      dft<32>(u);
+#pragma unroll
+      for (int r = 0; r < 32; r++) h[q][r] = __floats2half2_rn(u[r].x * SC, u[r].y * SC);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const int iv = tid + 512 * q;
+      const int k = iv & (R - 1);
+      const int j = (iv - k) * R + k;
+      __half2 *b = buf + j + j / R;
+#pragma unroll
+      for (int r = 0; r < 32; r++) b[r * (R + 1)] = h[q][r];
+    }
+  }
+  __syncthreads();
+  // ---- pass 2: radix 32, span NB; outputs c = iv + NB r go straight to global
+  constexpr int RKEEP = CPLX ? R : R / 2;  // real data keeps channels c < N/2
+  const float oscale = prm.out_scale * 1024.0f;  // undoes the two 2^-5 scalings exactly
+#pragma unroll 1
+  for (int q = 0; q < 2; q++) {
+    const int iv = tid + 512 * q;
+    float2 v[32];
+    const __half2 *b = buf + iv + iv / R;
+#pragma unroll
+    for (int r = 0; r < 32; r++) v[r] = __half22float2(b[r * (NB + NB / R)]);
+    twiddle<N, R, NB>(v, iv, prm.tw);
+    dft<32>(v);
+    const float2 fs = fsubt[iv & (FSUB - 1)];
+    OutT *o = out0 + (size_t)(iv >> 4) * ctile_stride + (iv & 15);
+#pragma unroll
+    for (int r = 0; r < RKEEP; r++) {
+      const float2 fr = cmul(fs, fstept[(iv / FSUB) + r * (NB / FSUB)]);
+      o[(size_t)r * (NB / 16) * ctile_stride] = to_out<OutT>(cmul(v[r], fr), oscale);
+    }
+  }
+}
+
+template <typename OutT, bool CPLX>
+static cudaError_t launch_fstage15h(const FParams &prm, int nt, cudaStream_t s) {
+  const Job &job = prm.job;
+  constexpr int NCHAN = CPLX ? F15 : F15 / 2;
+  if (job.F != F15 || job.nchan != NCHAN || job.stride != F15_STRIDE || job.substride != F15_SUB ||
+      job.fsub != NCHAN / F15_STRIDE)
+    return cudaErrorInvalidValue;
+  const size_t smem = sizeof(float2) * ((size_t)F15_SUB + 2 * F15_STRIDE + NCHAN / F15_STRIDE) +
+                      sizeof(__half2) * ((size_t)F15 + F15 / 32) + (CPLX ? 0 : (size_t)F15 / 2 + 48);
+  auto kern = fstage15h_kernel<OutT, CPLX>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (nt > 65535) return cudaErrorInvalidValue;
+  dim3 grid(2u * (unsigned)job.nant, (unsigned)nt, 1u);
+  kern<<<grid, 512, smem, s>>>(prm);
+  return cudaGetLastError();
+}
+
 template <typename OutT, bool CPLX>
 static cudaError_t launch_fstage_l(const FParams &prm, int nt, cudaStream_t s) {
   switch (prm.job.log2F) {
@@ -759,7 +929,9 @@ static cudaError_t launch_fstage_l(const FParams &prm, int nt, cudaStream_t s) {
     case 12: return launch_fstage_t<12, OutT, CPLX>(prm, nt, s);
     case 13: return launch_fstage_t<13, OutT, CPLX>(prm, nt, s);
     case 14: return launch_fstage_t<14, OutT, CPLX>(prm, nt, s);
-    case 15: return launch_fstage_cluster<OutT, CPLX>(prm, nt, s);
+    case 15:  // FP32 output: the 2-CTA cluster kernel; FP16 / FP8 output: one CTA with an FP16 buffer
+      if constexpr (std::is_same<OutT, float2>::value) return launch_fstage_cluster<OutT, CPLX>(prm, nt, s);
+      else return launch_fstage15h<OutT, CPLX>(prm, nt, s);
     default: return cudaErrorInvalidValue;
   }
 }
