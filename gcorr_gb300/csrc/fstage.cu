@@ -750,20 +750,45 @@ static cudaError_t launch_fstage_cluster(const FParams &prm, int nt, cudaStream_
   return cudaGetLastError();
 }
 
-// ---------------------------------- 32768-point windows, FP16 / FP8 channelised output
-// One CTA per (pol, FFT), 512 threads, three radix-32 passes over n = iv + 1024 r; each
-// thread owns two 32-point groups (iv = tid, tid + 512) per pass.  The intermediate
-// spectrum lives in shared memory as FP16 (135 KB instead of 256 KB in FP32, so no
-// cluster is needed), scaled by 2^-5 after each of the first two passes: for any input
-// (|x| <= 127*sqrt(2)) the stored values stay below 6000, far inside FP16's range, and the
-// two extra roundings (2^-11 relative) sit below the FP16 / FP8 output rounding.  The
-// scale is undone exactly in the final cast.  In the in-place middle pass every thread
-// keeps its first group's results as half2 registers until the barrier that ends all reads.
-template <typename OutT, bool CPLX>
-__global__ void __launch_bounds__(512, 1) fstage15h_kernel(FParams prm) {
-  constexpr int N = F15, R = 32, NB = N / R, PADN = N + N / R;
-  constexpr int NCHAN = CPLX ? N : N / 2;
-  constexpr int STRIDE = F15_STRIDE, SUB = F15_SUB, FSUB = NCHAN / STRIDE;
+// ------------------------ 16384- and 32768-point windows, FP16 / FP8 channelised output
+// One CTA per (pol, FFT) with N/64 threads; passes of radix 32, 32 and N/1024 over
+// n = iv + (N/R) r, each thread owning two 32-point groups in the first two passes (and
+// two or four butterflies in the last).  The intermediate spectrum lives in shared memory
+// as FP16 (N*4 bytes instead of N*8: one CTA holds a 32768-point window without a cluster,
+// and two 16384-point CTAs share an SM), scaled by 2^-5 after each of the first two passes:
+// for any input (|x| <= 127*sqrt(2)) the stored values stay below 6000, far inside FP16's
+// range, and the two extra roundings (2^-11 relative) sit below the FP16 / FP8 output
+// rounding.  The scale is undone exactly in the final cast.  In the in-place middle pass
+// every thread keeps its first group's results as half2 registers until the barrier that
+// ends all reads.
+// rotator / frac-delay table split for FFT length 2^L (fxkernel.cpp:57-64 for square nchan)
+template <int L, bool CPLX>
+struct TPlan {
+  static constexpr int N = 1 << L;
+  static constexpr int NCHAN = CPLX ? N : N / 2;
+  static constexpr int STRIDE = 1 << (log2c(NCHAN) / 2);
+  static constexpr int SUB = N / STRIDE;
+  static constexpr int FSUB = NCHAN / STRIDE;
+};
+
+template <int L>
+struct HPlan {
+  static constexpr int N = 1 << L;
+  static constexpr int NT = N / 64;                  // threads: two 32-point groups each
+  static constexpr int R = 32, RL = N / (32 * 32);   // radix of passes 0, 1 and of the last pass
+  static constexpr int NB = N / R, NBL = N / RL;
+  static constexpr int PADN = N + N / R;
+  static constexpr int GL = NBL / NT;                // last-pass butterflies per thread
+  static constexpr int MINB = L >= 15 ? 1 : 2;
+};
+
+template <int L, typename OutT, bool CPLX>
+__global__ void __launch_bounds__(HPlan<L>::NT, HPlan<L>::MINB) fstage_h_kernel(FParams prm) {
+  using H = HPlan<L>;
+  using Pl = TPlan<L, CPLX>;
+  constexpr int N = H::N, NT = H::NT, R = H::R, RL = H::RL, NB = H::NB, NBL = H::NBL, PADN = H::PADN;
+  constexpr int NCHAN = Pl::NCHAN, STRIDE = Pl::STRIDE, SUB = Pl::SUB, FSUB = Pl::FSUB;
+  static_assert(NB % SUB == 0 && NBL % FSUB == 0 && NBL % 16 == 0, "table splits / channel tiles");
   constexpr float SC = 1.0f / 32.0f;
   const Job &job = prm.job;
   extern __shared__ float2 smem[];
@@ -787,7 +812,7 @@ __global__ void __launch_bounds__(512, 1) fstage15h_kernel(FParams prm) {
   const size_t ctile_stride = (size_t)prm.T * nstreams * CW;
   if (!g.valid) {
     const OutT z = to_out<OutT>(make_float2(0.f, 0.f), 1.f);
-    for (int c = tid; c < NCHAN; c += 512) out0[(size_t)(c >> 4) * ctile_stride + (c & 15)] = z;
+    for (int c = tid; c < NCHAN; c += NT) out0[(size_t)(c >> 4) * ctile_stride + (c & 15)] = z;
     return;
   }
   const long long off = g.offset;
@@ -800,21 +825,21 @@ __global__ void __launch_bounds__(512, 1) fstage15h_kernel(FParams prm) {
     const long long last = (off + N + 1) >> 1;
     const int nvec = (int)((last - stage_base + 15) >> 4);
     uint4 *dst = reinterpret_cast<uint4 *>(stage);
-    for (int i = tid; i < nvec; i += 512) dst[i] = __ldg(&src[i]);
+    for (int i = tid; i < nvec; i += NT) dst[i] = __ldg(&src[i]);
   }
-  for (int k = tid; k < SUB; k += 512) {
+  for (int k = tid; k < SUB; k += NT) {
     float sn, cs;
     sincospif(-2.0f * fmaf((float)k, g.c1, g.c0), &sn, &cs);
     tsub[k] = make_float2(cs, sn);
   }
-  for (int i = tid; i < STRIDE; i += 512) {
+  for (int i = tid; i < STRIDE; i += NT) {
     float sn, cs;
     sincospif(-2.0f * ((float)i * g.cstep), &sn, &cs);
     tstep[i] = make_float2(cs, sn);
     sincospif(2.0f * ((float)(i * FSUB) * g.cf), &sn, &cs);
     fstept[i] = make_float2(cs, sn);
   }
-  for (int k = tid; k < FSUB; k += 512) {
+  for (int k = tid; k < FSUB; k += NT) {
     float sn, cs;
     sincospif(2.0f * ((float)k * g.cf), &sn, &cs);
     fsubt[k] = make_float2(cs, sn);
@@ -824,7 +849,7 @@ __global__ void __launch_bounds__(512, 1) fstage15h_kernel(FParams prm) {
   // ---- pass 0 (span 1): decode + fringe-rotate, radix 32 over n = iv + NB r
 #pragma unroll 1
   for (int q = 0; q < 2; q++) {
-    const int iv = tid + 512 * q;
+    const int iv = tid + NT * q;
     float2 u[32];
     const float2 rs = tsub[iv & (SUB - 1)];  // n mod SUB = iv mod SUB
     if constexpr (CPLX) {
@@ -857,7 +882,7 @@ __global__ void __launch_bounds__(512, 1) fstage15h_kernel(FParams prm) {
     __half2 h[2][32];
 #pragma unroll
     for (int q = 0; q < 2; q++) {
-      const int iv = tid + 512 * q;
+      const int iv = tid + NT * q;
       float2 u[32];
       const __half2 *b = buf + iv + iv / R;
 #pragma unroll
@@ -870,7 +895,7 @@ __global__ void __launch_bounds__(512, 1) fstage15h_kernel(FParams prm) {
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < 2; q++) {
-      const int iv = tid + 512 * q;
+      const int iv = tid + NT * q;
       const int k = iv & (R - 1);
       const int j = (iv - k) * R + k;
       __half2 *b = buf + j + j / R;
@@ -879,43 +904,44 @@ __global__ void __launch_bounds__(512, 1) fstage15h_kernel(FParams prm) {
     }
   }
   __syncthreads();
-  // ---- pass 2: radix 32, span NB; outputs c = iv + NB r go straight to global
-  constexpr int RKEEP = CPLX ? R : R / 2;  // real data keeps channels c < N/2
+  // ---- last pass: radix RL, span NBL; outputs c = iv + NBL r go straight to global
+  constexpr int RKEEP = CPLX ? RL : RL / 2;       // real data keeps channels c < N/2
   const float oscale = prm.out_scale * 1024.0f;  // undoes the two 2^-5 scalings exactly
 #pragma unroll 1
-  for (int q = 0; q < 2; q++) {
-    const int iv = tid + 512 * q;
-    float2 v[32];
+  for (int q = 0; q < H::GL; q++) {
+    const int iv = tid + NT * q;
+    float2 v[RL];
     const __half2 *b = buf + iv + iv / R;
 #pragma unroll
-    for (int r = 0; r < 32; r++) v[r] = __half22float2(b[r * (NB + NB / R)]);
-    twiddle<N, R, NB>(v, iv, prm.tw);
-    dft<32>(v);
+    for (int r = 0; r < RL; r++) v[r] = __half22float2(b[r * (NBL + NBL / R)]);
+    twiddle<N, RL, NBL>(v, iv, prm.tw);
+    dft<RL>(v);
     const float2 fs = fsubt[iv & (FSUB - 1)];
     OutT *o = out0 + (size_t)(iv >> 4) * ctile_stride + (iv & 15);
 #pragma unroll
     for (int r = 0; r < RKEEP; r++) {
-      const float2 fr = cmul(fs, fstept[(iv / FSUB) + r * (NB / FSUB)]);
-      o[(size_t)r * (NB / 16) * ctile_stride] = to_out<OutT>(cmul(v[r], fr), oscale);
+      const float2 fr = cmul(fs, fstept[(iv / FSUB) + r * (NBL / FSUB)]);
+      o[(size_t)r * (NBL / 16) * ctile_stride] = to_out<OutT>(cmul(v[r], fr), oscale);
     }
   }
 }
 
-template <typename OutT, bool CPLX>
-static cudaError_t launch_fstage15h(const FParams &prm, int nt, cudaStream_t s) {
+template <int L, typename OutT, bool CPLX>
+static cudaError_t launch_fstage_h(const FParams &prm, int nt, cudaStream_t s) {
+  using H = HPlan<L>;
+  using Pl = TPlan<L, CPLX>;
   const Job &job = prm.job;
-  constexpr int NCHAN = CPLX ? F15 : F15 / 2;
-  if (job.F != F15 || job.nchan != NCHAN || job.stride != F15_STRIDE || job.substride != F15_SUB ||
-      job.fsub != NCHAN / F15_STRIDE)
+  if (job.F != H::N || job.nchan != Pl::NCHAN || job.stride != Pl::STRIDE || job.substride != Pl::SUB ||
+      job.fsub != Pl::FSUB || job.fstride != Pl::STRIDE)
     return cudaErrorInvalidValue;
-  const size_t smem = sizeof(float2) * ((size_t)F15_SUB + 2 * F15_STRIDE + NCHAN / F15_STRIDE) +
-                      sizeof(__half2) * ((size_t)F15 + F15 / 32) + (CPLX ? 0 : (size_t)F15 / 2 + 48);
-  auto kern = fstage15h_kernel<OutT, CPLX>;
+  const size_t smem = sizeof(float2) * ((size_t)Pl::SUB + 2 * Pl::STRIDE + Pl::FSUB) +
+                      sizeof(__half2) * (size_t)H::PADN + (CPLX ? 0 : (size_t)H::N / 2 + 48);
+  auto kern = fstage_h_kernel<L, OutT, CPLX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if (nt > 65535) return cudaErrorInvalidValue;
   dim3 grid(2u * (unsigned)job.nant, (unsigned)nt, 1u);
-  kern<<<grid, 512, smem, s>>>(prm);
+  kern<<<grid, H::NT, smem, s>>>(prm);
   return cudaGetLastError();
 }
 
@@ -928,10 +954,12 @@ static cudaError_t launch_fstage_l(const FParams &prm, int nt, cudaStream_t s) {
     case 11: return launch_fstage_t<11, OutT, CPLX>(prm, nt, s);
     case 12: return launch_fstage_t<12, OutT, CPLX>(prm, nt, s);
     case 13: return launch_fstage_t<13, OutT, CPLX>(prm, nt, s);
-    case 14: return launch_fstage_t<14, OutT, CPLX>(prm, nt, s);
+    case 14:  // FP32 output: FP32 shared buffer; FP16 / FP8 output: FP16 buffer, two CTAs per SM
+      if constexpr (std::is_same<OutT, float2>::value) return launch_fstage_t<14, OutT, CPLX>(prm, nt, s);
+      else return launch_fstage_h<14, OutT, CPLX>(prm, nt, s);
     case 15:  // FP32 output: the 2-CTA cluster kernel; FP16 / FP8 output: one CTA with an FP16 buffer
       if constexpr (std::is_same<OutT, float2>::value) return launch_fstage_cluster<OutT, CPLX>(prm, nt, s);
-      else return launch_fstage15h<OutT, CPLX>(prm, nt, s);
+      else return launch_fstage_h<15, OutT, CPLX>(prm, nt, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -107,15 +107,16 @@ def test_fp16_channelised_vs_fp64():
     assert err.max() < FP16_TOL, err.max()
 
 
+@pytest.mark.parametrize("fft_len", [16384, 32768])
 @pytest.mark.parametrize("is_complex", [True, False])
 @pytest.mark.parametrize("precision", ["fp16", "fp8"])
-def test_32768_point_reduced_precision_vs_fp64(is_complex, precision):
-    """32768-point windows with FP16 or FP8 channelised data go through the one-CTA F-stage
+def test_large_fft_reduced_precision_vs_fp64(fft_len, is_complex, precision):
+    """16384- and 32768-point windows with FP16 or FP8 channelised data go through the F-stage
     whose intermediate spectrum is held in FP16 shared memory (two extra 2^-11 roundings).
     FP16 must stay within the FP16 tolerance of the FP64 oracle.  FP8: crosses within 6 % (the
     E4M3 bound of the other FP8 tests); the power spectra's E4M3 rounding error only averages
     over the 8 FFTs here (1 % holds for 200 FFTs; about 2.3 % is expected for 8), bound 3.5 %."""
-    nchan = 32768 if is_complex else 16384
+    nchan = fft_len if is_complex else fft_len // 2
     w = synth.Workload(nant=3, nchan=nchan, nfft=8, nbit=8 if is_complex else 2, is_complex=is_complex,
                        bw_hz=64e6, rho=0.3, seed=321 + int(is_complex))
     d = synth.generate(w)
