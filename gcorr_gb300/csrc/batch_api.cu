@@ -5,7 +5,10 @@
 // job once eagerly (module loading, kernel attributes, validation), then
 // captures all jobs' launch sequences as parallel branches of one graph: a
 // launch of the batch is a single cudaGraphLaunch, and the GPU overlaps the
-// jobs' kernels.  Inputs and delay models are fixed at creation (their upload
+// jobs' kernels.  Jobs on pinned host inputs copy them one job after another
+// (each job's copies wait for the previous job's), so that the first jobs
+// correlate while the later ones load, instead of every job sharing the host
+// link until all copies end together.  Inputs and delay models are fixed at creation (their upload
 // copies read pinned staging that the graph replays); build a new batch to
 // change them.
 #include <stdio.h>
@@ -19,6 +22,7 @@ struct gxc_batch {
   std::vector<gxc_handle *> handles;
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> events;
+  std::vector<cudaEvent_t> copied;  // per job: its input copies are done
   cudaStream_t origin = nullptr;
   cudaEvent_t fork = nullptr;
   cudaGraph_t graph = nullptr;
@@ -33,6 +37,7 @@ void destroy_batch(gxc_batch *b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   for (cudaEvent_t e : b->events) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->copied) cudaEventDestroy(e);
   for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->origin) cudaStreamDestroy(b->origin);
@@ -79,6 +84,9 @@ gxc_status gxc_batch_create(const gxc_job *jobs, int njobs, gxc_batch **out) {
     if (e == cudaSuccess) b->streams.push_back(s);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (e == cudaSuccess) b->events.push_back(ev);
+    cudaEvent_t cp;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&cp, cudaEventDisableTiming);
+    if (e == cudaSuccess) b->copied.push_back(cp);
   }
   if (e != cudaSuccess) return batch_fail(b, GXC_ERR_CUDA, cudaGetErrorString(e));
   // capture: fork every job onto its own stream, join back to the origin
@@ -87,7 +95,8 @@ gxc_status gxc_batch_create(const gxc_job *jobs, int njobs, gxc_batch **out) {
   for (int i = 0; e == cudaSuccess && i < njobs; i++) {
     e = cudaStreamWaitEvent(b->streams[i], b->fork, 0);
     if (e != cudaSuccess) break;
-    gxc_status st = gxc_process(b->handles[i], b->streams[i]);
+    gxc_status st = gxc::process_chained(b->handles[i], b->streams[i], i > 0 ? b->copied[i - 1] : nullptr,
+                                         b->copied[i]);
     if (st != GXC_OK) {
       cudaGraph_t g = nullptr;
       cudaStreamEndCapture(b->origin, &g);

@@ -452,7 +452,12 @@ __global__ void add_kernel(float *__restrict__ dst, const float *__restrict__ sr
   if (i < n) dst[i] += src[i];
 }
 
-gxc_status gxc_process(gxc_handle *h, void *stream) {
+gxc_status gxc_process(gxc_handle *h, void *stream) { return gxc::process_chained(h, stream, nullptr, nullptr); }
+
+// process() with its host->device input copies ordered behind copy_wait (when given) and
+// followed by a record of copy_done (when given); batches use it to chain the jobs' copies.
+extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEvent_t copy_wait,
+                                             cudaEvent_t copy_done) {
   if (!h) return GXC_ERR_INVALID_ARGUMENT;
   if (!h->have_input) return fail(h, GXC_ERR_STATE, "process() before set_input()");
   if (!h->have_delays) return fail(h, GXC_ERR_STATE, "process() before set_delays()");
@@ -488,12 +493,14 @@ gxc_status gxc_process(gxc_handle *h, void *stream) {
     launches++;
   }
   if (h->input_on_host) {
+    if (copy_wait) GXC_CUDA(h, cudaStreamWaitEvent(s, copy_wait, 0), "ordering the input copies");
     for (int a = 0; a < nant; a++)
       GXC_CUDA(h,
                cudaMemcpyAsync(h->d_inbuf + (size_t)a * h->bytes_per_ant, h->user_ptrs[a], h->bytes_per_ant,
                                cudaMemcpyHostToDevice, s),
                "copying input to the device");
   }
+  if (copy_done) GXC_CUDA(h, cudaEventRecordWithFlags(copy_done, s, rec_flags), "recording the input copies");
   if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_begin, s), "timing event");
 
   GXC_CUDA(h, launch_geometry(h->job, s), "geometry kernel");

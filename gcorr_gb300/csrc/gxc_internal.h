@@ -86,6 +86,10 @@ int xstage_tensor_channels_per_cta(int nant, int chan_type);
 int xstage_tensor_fits(int nant, int nchan, int chan_type);
 cudaError_t xstage_tensor_take_error(int *flag);
 
+// gxc_api.cu: process() with its host->device input copies ordered behind copy_wait (when not
+// null) and followed by a record of copy_done (when not null).
+gxc_status process_chained(gxc_handle *h, void *stream, cudaEvent_t copy_wait, cudaEvent_t copy_done);
+
 // Output baseline index of antennas j <= k (crosses in fxkernel order, then autos).
 __host__ __device__ inline int baseline_index(int j, int k, int nant) {
   if (j == k) return nant * (nant - 1) / 2 + j;
