@@ -373,6 +373,7 @@ def main():
     ap.add_argument("--x-engine", default="auto", choices=["auto", "cuda_core", "tensor"])
     ap.add_argument("--fft-block", type=int, default=0)
     ap.add_argument("--nfft", type=int, default=0, help="override the FFT count (small profiling captures)")
+    ap.add_argument("--nchan", type=int, default=0, help="override the channel count (small profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-xcompare", action="store_true")
@@ -398,6 +399,8 @@ def main():
     w = synth.Workload(**{**workload(args.config).__dict__, "seed": 1234 + 7919 * rank})
     if args.nfft > 0:
         w = synth.Workload(**{**w.__dict__, "nfft": args.nfft})
+    if args.nchan > 0:
+        w = synth.Workload(**{**w.__dict__, "nchan": args.nchan})
     tg = time.perf_counter()
     d = synth.generate(w, device=dev)
     torch.cuda.synchronize()

@@ -25,6 +25,8 @@
 #include <cuda.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "gxc_internal.h"
 
 namespace gxc {
@@ -998,6 +1000,244 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big_kernel(Params p) {
   if (warp == NPROD_WARPS) tmem_dealloc(tmem, 512);
 }
 
+// FP16 / FP8 path for 33..64 antennas with two CTA types in one launch; the Gram matrix
+// P P^T of a channel (256 rows: re/im of every stream) is split into D_top = P[0:128] P^T
+// (N = 256) and D_bot = P[128:256] P[128:256]^T (N = 128), as in the kernel above, but the two
+// parts are computed by different CTAs so each CTA covers more channels in its 512 TMEM columns:
+//   top CTAs (blockIdx < nchan/2): channels 2b, 2b+1, D_top of each (256 columns each), loading
+//     all streams of both channels (8-byte FP16 / 4-byte FP8 gathers);
+//   bottom CTAs: channels 4b..4b+3, D_bot of each (128 columns each), loading the bottom 64
+//     streams of the four channels (16-byte FP16 / 8-byte FP8 gathers).
+// A 32-byte sector read from L2 then carries 2 or 4 useful channels instead of 1: 2.5 KB of
+// sectors per channel and FFT instead of 4 KB.
+constexpr int B2_STAGES = 3;
+constexpr int B2_STAGE_BYTES = 65536;  // top: 2 channels x 256 rows; bottom: 4 channels x 128 rows (128 B each)
+
+// Producer body: NCH channels from c0 (within one 16-channel tile), streams [s_lo, n), operand
+// rows of channel ci at ci*ROWS + 2*(s - s_lo) (re) and +1 (im).
+template <bool F8, int NCH, int ROWS>
+__device__ __forceinline__ void big2_produce(const Params &p, unsigned char *stage, int c0, int s_lo, int tb,
+                                             int tid) {
+  constexpr int NL = F8 ? 16 : 8;  // loads (FFTs) per task
+  constexpr int U = NCH == 2 ? 4 : 2;
+  using V = typename std::conditional<F8, typename std::conditional<NCH == 2, uint32_t, uint2>::type,
+                                      typename std::conditional<NCH == 2, uint2, uint4>::type>::type;
+  const int n = p.nstream;
+  const int ns = n - s_lo;
+  const int ntask = 8 * ns;  // (stream, 16-byte K chunk of a row)
+  const size_t esz = F8 ? 2 : 4;
+  const unsigned char *src = (const unsigned char *)p.chan + (((size_t)(c0 >> 4) * p.T * n) * CW + (c0 & 15)) * esz;
+  for (int task0 = tid; task0 < ntask; task0 += U * NPROD) {
+    V w[U][NL];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int task = task0 + u * NPROD;
+      const int s = s_lo + task % ns;
+      const int o = task / ns;
+#pragma unroll
+      for (int i = 0; i < NL; i++) {
+        const int t = tb + NL * o + i;
+        if (task < ntask && t < p.nt) {
+          w[u][i] = __ldg(reinterpret_cast<const V *>(src + ((size_t)t * n + s) * CW * esz));
+        } else {
+          w[u][i] = V{};
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int task = task0 + u * NPROD;
+      if (task >= ntask) break;
+      const int s = s_lo + task % ns;
+      const int o = task / ns;
+      const int sr = s - s_lo;
+      const int sw = (sr >> 2) & 1;  // lanes s..s+7 store their first row at 8 swizzle positions
+#pragma unroll
+      for (int ci = 0; ci < NCH; ci++) {
+        uint4 re, im;
+        if constexpr (F8) {
+          // channel ci's (re, im) byte pair of FFT i, two FFTs per word: re(2i), im(2i), re(2i+1), im(2i+1)
+          uint32_t x[8];
+#pragma unroll
+          for (int i = 0; i < 8; i++) {
+            uint32_t a, b2;
+            if constexpr (NCH == 2) {
+              a = w[u][2 * i];
+              b2 = w[u][2 * i + 1];
+            } else {
+              a = ci < 2 ? w[u][2 * i].x : w[u][2 * i].y;
+              b2 = ci < 2 ? w[u][2 * i + 1].x : w[u][2 * i + 1].y;
+            }
+            x[i] = prmt(a, b2, (ci & 1) ? 0x7632u : 0x5410u);
+          }
+          re = make_uint4(prmt(x[0], x[1], 0x6420), prmt(x[2], x[3], 0x6420), prmt(x[4], x[5], 0x6420),
+                          prmt(x[6], x[7], 0x6420));
+          im = make_uint4(prmt(x[0], x[1], 0x7531), prmt(x[2], x[3], 0x7531), prmt(x[4], x[5], 0x7531),
+                          prmt(x[6], x[7], 0x7531));
+        } else {
+          uint32_t x[8];
+#pragma unroll
+          for (int i = 0; i < 8; i++) {
+            if constexpr (NCH == 2) x[i] = ci ? w[u][i].y : w[u][i].x;
+            else x[i] = ci == 0 ? w[u][i].x : ci == 1 ? w[u][i].y : ci == 2 ? w[u][i].z : w[u][i].w;
+          }
+          re = make_uint4(prmt(x[0], x[1], 0x5410), prmt(x[2], x[3], 0x5410), prmt(x[4], x[5], 0x5410),
+                          prmt(x[6], x[7], 0x5410));
+          im = make_uint4(prmt(x[0], x[1], 0x7632), prmt(x[2], x[3], 0x7632), prmt(x[4], x[5], 0x7632),
+                          prmt(x[6], x[7], 0x7632));
+        }
+        const int ra = ci * ROWS + 2 * sr + sw, rb = ci * ROWS + 2 * sr + 1 - sw;
+        *reinterpret_cast<uint4 *>(stage + ra * 128 + ((o ^ (ra & 7)) << 4)) = sw ? im : re;
+        *reinterpret_cast<uint4 *>(stage + rb * 128 + ((o ^ (rb & 7)) << 4)) = sw ? re : im;
+      }
+    }
+  }
+}
+
+// Epilogue of one channel's TMEM block: rows (TMEM lanes) are streams s_lo + row/2 (re/im by
+// row parity), columns npc*16 starting at col0 are streams s2_lo + col/2.
+__device__ __forceinline__ void big2_epilogue(const Params &p, uint32_t tmem, int warp, int lane, int c, int s_lo,
+                                              int s2_lo, uint32_t col0, int npc) {
+  const int n = p.nstream;
+  const int arow = 32 * warp + lane;
+  const int s1 = s_lo + (arow >> 1), part1 = arow & 1;
+  const int j = s1 >> 1, l = s1 & 1;
+  for (int pc = 0; pc < npc; pc++) {
+    __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skips below
+    float v[16], pv[16];
+    tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + col0 + 16u * pc, v);
+#pragma unroll
+    for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
+    if (s1 >= n) continue;
+    const int s2b = s2_lo + 8 * pc;
+#pragma unroll
+    for (int qq = 0; qq < 4; qq++) {
+      const int q = qq + 4 * part1;
+      const int s2 = s2b + q;
+      if (s2 >= n) continue;
+      const int k = s2 >> 1, m = s2 & 1;
+      if (j > k || (j == k && !p.autos)) continue;
+      float re, im;
+      if (part1 == 0) {
+        re = v[2 * q] + pv[2 * q + 1];
+        im = pv[2 * q] - v[2 * q + 1];
+      } else {
+        re = pv[2 * q] + v[2 * q + 1];
+        im = v[2 * q] - pv[2 * q + 1];
+      }
+      const int bl = baseline_index(j, k, p.nant);
+      const size_t o = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
+      float2 sm = p.vsum[o], e = p.vcomp[o];
+      two_sum_add(sm.x, e.x, re);
+      two_sum_add(sm.y, e.y, im);
+      p.vsum[o] = sm;
+      p.vcomp[o] = e;
+    }
+  }
+}
+
+template <bool F8>
+__global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big2_kernel(Params p) {
+  constexpr int KC = F8 ? 128 : 64, KSTEP = F8 ? 32 : 16;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar_full[B2_STAGES], bar_empty[B2_STAGES], bar_done;
+  __shared__ uint32_t tmem_base_sh;
+  unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t sbase = smem_u32(smem);
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int n = p.nstream;
+  const int nchunks = (p.nt + KC - 1) / KC;
+  const int ntop = p.nchan / 2;
+  const bool top = (int)blockIdx.x < ntop;
+  const int nch = top ? 2 : 4;
+  const int c0 = top ? 2 * (int)blockIdx.x : 4 * ((int)blockIdx.x - ntop);
+  const int rows = top ? 256 : 128;  // operand rows per channel
+  const int s_lo = top ? 0 : 64;      // first stream of the loaded rows
+
+  {  // zero the padding rows (streams n..) of every channel block of every stage
+    const int used = 2 * (n - s_lo), pad = rows - used;
+    if (pad > 0) {
+      const int per_stage = nch * pad * 8;  // 16-byte words
+      for (int i = tid; i < B2_STAGES * per_stage; i += NTHREADS) {
+        const int st = i / per_stage, r0 = i - st * per_stage;
+        const int w = r0 & 7, rr = r0 >> 3;
+        const int ci = rr / pad, row = ci * rows + used + (rr - ci * pad);
+        *reinterpret_cast<uint4 *>(smem + (size_t)st * B2_STAGE_BYTES + row * 128 + w * 16) = make_uint4(0, 0, 0, 0);
+      }
+    }
+  }
+  if (tid == 0) {
+    for (int s = 0; s < B2_STAGES; s++) {
+      mbar_init(smem_u32(&bar_full[s]), NPROD);
+      mbar_init(smem_u32(&bar_empty[s]), 1);
+    }
+    mbar_init(smem_u32(&bar_done), 1);
+    fence_mbar_init();
+  }
+  if (warp == NPROD_WARPS) {
+    tmem_alloc(smem_u32(&tmem_base_sh), 512);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+
+  if (warp < NPROD_WARPS) {
+    for (int ch = 0; ch < nchunks; ch++) {
+      const int st = ch % B2_STAGES;
+      if (ch >= B2_STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / B2_STAGES) - 1) & 1, p.err)) break;
+      unsigned char *stage = smem + (size_t)st * B2_STAGE_BYTES;
+      if (top) big2_produce<F8, 2, 256>(p, stage, c0, 0, ch * KC, tid);
+      else big2_produce<F8, 4, 128>(p, stage, c0, 64, ch * KC, tid);
+      fence_proxy_async_smem();
+      mbar_arrive(smem_u32(&bar_full[st]));
+    }
+  } else if (lane == 0) {
+    // ------------------------------------------------------------ MMA issuer
+    for (int ch = 0; ch < nchunks; ch++) {
+      const int st = ch % B2_STAGES;
+      if (!mbar_wait(smem_u32(&bar_full[st]), (ch / B2_STAGES) & 1, p.err)) break;
+      tc_fence_after();
+      const uint32_t sa = sbase + st * B2_STAGE_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < KC / KSTEP; kk++) {
+        const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
+        for (int ci = 0; ci < nch; ci++) {
+          const uint64_t d = desc_sw128(sa + ci * rows * 128 + kk * 32);
+          if (top) {  // rows 0..127 of the channel's 256 against all 256: D_top, 256 columns
+            if constexpr (F8) mma_f8(tmem + ci * 256, d, d, IDESC_N256, acc);
+            else mma_f16(tmem + ci * 256, d, d, IDESC_N256, acc);
+          } else {    // the channel's 128 bottom rows against themselves: D_bot, 128 columns
+            if constexpr (F8) mma_f8(tmem + ci * 128, d, d, IDESC, acc);
+            else mma_f16(tmem + ci * 128, d, d, IDESC, acc);
+          }
+        }
+      }
+      mma_commit(smem_u32(&bar_empty[st]));
+    }
+    mma_commit(smem_u32(&bar_done));
+    mbar_wait(smem_u32(&bar_done), 0, p.err);  // issued MMAs drained before TMEM is read or freed
+  }
+
+  if (warp < 4) {
+    const bool ok = mbar_wait(smem_u32(&bar_done), 0, p.err);
+    tc_fence_after();
+    if (ok) {
+      for (int ci = 0; ci < nch; ci++) {
+        if (top) big2_epilogue(p, tmem, warp, lane, c0 + ci, 0, 0, (uint32_t)(ci * 256), 16);
+        else big2_epilogue(p, tmem, warp, lane, c0 + ci, 64, 64, (uint32_t)(ci * 128), 8);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == NPROD_WARPS) tmem_dealloc(tmem, 512);
+}
+
 }  // namespace tc
 
 // two rows (re, im) per stream, two streams per antenna: up to 32 antennas fill one
@@ -1109,6 +1349,15 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   if (e != cudaSuccess) return e;
   if (R > 128) {
     const size_t bsmem = (size_t)tc::BIG_STAGES * tc::BIG_STAGE_BYTES + 1024;
+    if (nchan % 4 == 0) {
+      // top CTAs (2 channels, D_top) then bottom CTAs (4 channels, D_bot) in one launch
+      const size_t b2smem = (size_t)tc::B2_STAGES * tc::B2_STAGE_BYTES + 1024;
+      auto kern2 = chan_type == CHAN_F8 ? tc::xstage_tc_big2_kernel<true> : tc::xstage_tc_big2_kernel<false>;
+      e = cudaFuncSetAttribute(kern2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b2smem);
+      if (e != cudaSuccess) return e;
+      kern2<<<nchan / 2 + nchan / 4, tc::NTHREADS, b2smem, s>>>(p);
+      return cudaGetLastError();
+    }
     auto kern = chan_type == CHAN_F8 ? tc::xstage_tc_big_kernel<true> : tc::xstage_tc_big_kernel<false>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
     if (e != cudaSuccess) return e;
