@@ -528,6 +528,8 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
 // indexed at compile time.
 constexpr int NEPI_WARPS = 4;
 constexpr int NTHREADS_SPLIT = NPROD + 32 + NEPI_WARPS * 32 + 32;  // + TMA warp (the last)
+// 14 warps put 4 on one of the SM's four 16K-register sub-partitions: at most 128 registers
+// per thread (the R = 128 epilogue's 128 register sums then spill a little)
 constexpr int TMA_WARP_SPLIT = NPROD_WARPS + 1 + NEPI_WARPS;
 
 template <int R>
@@ -1004,9 +1006,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big_kernel(Params p) {
 // P P^T of a channel (256 rows: re/im of every stream) is split into D_top = P[0:128] P^T
 // (N = 256) and D_bot = P[128:256] P[128:256]^T (N = 128), as in the kernel above, but the two
 // parts are computed by different CTAs so each CTA covers more channels in its 512 TMEM columns:
-//   top CTAs (blockIdx < nchan/2): channels 2b, 2b+1, D_top of each (256 columns each), loading
+//   top CTAs (2 of every 3 blocks): 2 channels, D_top of each (256 columns each), loading
 //     all streams of both channels (8-byte FP16 / 4-byte FP8 gathers);
-//   bottom CTAs: channels 4b..4b+3, D_bot of each (128 columns each), loading the bottom 64
+//   bottom CTAs (every third block): 4 channels, D_bot of each (128 columns each), loading the bottom 64
 //     streams of the four channels (16-byte FP16 / 8-byte FP8 gathers).
 // A 32-byte sector read from L2 then carries 2 or 4 useful channels instead of 1: 2.5 KB of
 // sectors per channel and FFT instead of 4 KB.
@@ -1019,7 +1021,7 @@ template <bool F8, int NCH, int ROWS>
 __device__ __forceinline__ void big2_produce(const Params &p, unsigned char *stage, int c0, int s_lo, int tb,
                                              int tid) {
   constexpr int NL = F8 ? 16 : 8;  // loads (FFTs) per task
-  constexpr int U = NCH == 2 ? 4 : 2;
+  constexpr int U = NCH == 2 ? 4 : 2;  // tasks per thread with all their gathers in flight (8 gave 5-17 % less)
   using V = typename std::conditional<F8, typename std::conditional<NCH == 2, uint32_t, uint2>::type,
                                       typename std::conditional<NCH == 2, uint2, uint4>::type>::type;
   const int n = p.nstream;
@@ -1148,10 +1150,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big2_kernel(Params p) {
   const int warp = tid >> 5, lane = tid & 31;
   const int n = p.nstream;
   const int nchunks = (p.nt + KC - 1) / KC;
-  const int ntop = p.nchan / 2;
-  const bool top = (int)blockIdx.x < ntop;
+  // blocks 3g, 3g+1: top CTAs of channels 4g..4g+1 and 4g+2..4g+3; block 3g+2: the bottom CTA of
+  // channels 4g..4g+3.  The three run together and share the group's sectors in L2 (the bottom
+  // streams are read by both kinds)
+  const int grp = (int)blockIdx.x / 3, kind = (int)blockIdx.x - 3 * grp;
+  const bool top = kind < 2;
   const int nch = top ? 2 : 4;
-  const int c0 = top ? 2 * (int)blockIdx.x : 4 * ((int)blockIdx.x - ntop);
+  const int c0 = 4 * grp + (top ? 2 * kind : 0);
   const int rows = top ? 256 : 128;  // operand rows per channel
   const int s_lo = top ? 0 : 64;      // first stream of the loaded rows
 
@@ -1350,7 +1355,7 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   if (R > 128) {
     const size_t bsmem = (size_t)tc::BIG_STAGES * tc::BIG_STAGE_BYTES + 1024;
     if (nchan % 4 == 0) {
-      // top CTAs (2 channels, D_top) then bottom CTAs (4 channels, D_bot) in one launch
+      // per group of 4 channels: two top CTAs (2 channels, D_top) and one bottom CTA (4 channels, D_bot)
       const size_t b2smem = (size_t)tc::B2_STAGES * tc::B2_STAGE_BYTES + 1024;
       auto kern2 = chan_type == CHAN_F8 ? tc::xstage_tc_big2_kernel<true> : tc::xstage_tc_big2_kernel<false>;
       e = cudaFuncSetAttribute(kern2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b2smem);
