@@ -528,9 +528,12 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
     if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b + 1], s), "timing event");
     if (h->nbl > 0) {
       if (h->xeng == GXC_XENGINE_TENSOR) {
+        // FP32 spectra go through the FP16 hi/lo split scaled by 2^-(log2F/2): a spectrum value is
+        // at most F * 128*sqrt(2) (8-bit complex; 2-bit real is below that), which after the scale
+        // is <= 2^ceil(log2F/2) * 182 <= 46592 < 65504, the FP16 maximum, for every F <= 32768.
         GXC_CUDA(h,
                  launch_xstage_tensor(h->d_chan, h->chan_type, nant, c.nchan, h->T, nt, c.autos, h->d_vsum,
-                                      h->d_vcomp, s),
+                                      h->d_vcomp, s, h->log2F / 2),
                  "tensor-core X-stage kernel");
       } else {
         GXC_CUDA(h,

@@ -244,6 +244,9 @@ struct Params {
   // TMA raw tiles (small-N kernels): box = rbx channels x nstream x rkc FFTs, rnbox boxes
   // (channel tiles) per raw chunk, rbox_bytes each
   int rbx, rnbox, rkc, rbox_bytes;
+  // FP16 hi/lo split (FP32 data of known scale): values are multiplied by split_sc (a power of
+  // two) before the split, and the Gram sums by split_unsc (its inverse squared) at the end
+  float split_sc, split_unsc;
 };
 
 // FP16 and FP8 paths: one accumulation over the whole FFT block (its TMEM rounding
@@ -532,13 +535,20 @@ constexpr int NTHREADS_SPLIT = NPROD + 32 + NEPI_WARPS * 32 + 32;  // + TMA warp
 // per thread (the R = 128 epilogue's 128 register sums then spill a little)
 constexpr int TMA_WARP_SPLIT = NPROD_WARPS + 1 + NEPI_WARPS;
 
-template <int R>
+// H16 = false: TF32 hi (top 11 significand bits) and lo halves, kind::tf32, 32 FFTs per stage.
+// H16 = true: FP16 hi and lo halves of the scaled value (the same 22 significand bits for
+// values in FP16's normal range; a subnormal lo only adds an absolute error near 2^-25),
+// kind::f16 at twice the tf32 rate and half the shared-memory bytes, 64 FFTs per stage.  Used
+// where the data's scale is known (the F-stage's output): FP16's exponent range must hold it.
+template <int R, bool H16>
 __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Params p,
                                                                             const __grid_constant__ CUtensorMap tmap) {
   using C = Cfg<true>;
-  constexpr int KC = C::KC, NG = C::NG, GROUP_BYTES = C::GROUP_BYTES, STAGE_BYTES = C::STAGE_BYTES;
+  constexpr int KC = H16 ? 64 : C::KC, KSTEP = H16 ? 16 : C::KSTEP;
+  constexpr int TKC = H16 ? 8 : 4;       // FFTs per 16-byte chunk of an operand row
+  constexpr int NG = C::NG, GROUP_BYTES = C::GROUP_BYTES, STAGE_BYTES = C::STAGE_BYTES;
   constexpr int NSET = 2, SET_COLS = NG * 128, TMEM_COLS = NSET * SET_COLS;  // 512
-  constexpr int DP = 4;                  // stages per drain period
+  constexpr int DP = 128 / KC;           // stages per drain period (128 FFTs)
   constexpr int GCH = 128 / R;           // channels per MMA group
   constexpr int WP = (R > 32 ? R : 32) / 16;  // 16-column pieces a warp reads per group
   constexpr int PP = R / 16;             // pieces in one channel block
@@ -594,21 +604,24 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
   tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
 
+  const int KCR = p.rkc;      // FFTs per raw chunk (divides KC)
+  const int RPO = KC / KCR;   // raw chunks per operand stage
+  const int nraw = nchunks * RPO;
   if (warp == TMA_WARP_SPLIT) {
     // ------------------------------------------------------------ TMA producer
-    // One lane streams the block through the raw ring (one raw chunk of KC FFTs per
-    // operand stage, one box per channel tile, rows past the block zero-filled).
+    // One lane streams the block through the raw ring (raw chunks of KCR FFTs, one box per
+    // channel tile, rows past the block zero-filled).
     if (lane == 0) {
       const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(p.rbx - 1)) : 0;
       const uint32_t raw_s = sbase + STAGES * STAGE_BYTES;
       int issued = 0;
-      for (int rc = 0; rc < nchunks; rc++) {
+      for (int rc = 0; rc < nraw; rc++) {
         const int rs = rc % RSTAGES;
         if (rc >= RSTAGES && !mbar_wait(smem_u32(&raw_empty[rs]), ((rc / RSTAGES) - 1) & 1, p.err)) break;
         const uint32_t bar = smem_u32(&raw_full[rs]);
         mbar_expect_tx(bar, (uint32_t)(p.rbox_bytes * p.rnbox));
         for (int j = 0; j < p.rnbox; j++)
-          tma_load_4d(raw_s + rs * RAW_BYTES + j * p.rbox_bytes, &tmap, x0, 0, rc * KC, (cb >> 4) + j, bar);
+          tma_load_4d(raw_s + rs * RAW_BYTES + j * p.rbox_bytes, &tmap, x0, 0, rc * KCR, (cb >> 4) + j, bar);
         issued = rc + 1;
       }
       for (int rc = issued > RSTAGES ? issued - RSTAGES : 0; rc < issued; rc++)
@@ -616,78 +629,105 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
     }
   } else if (warp < NPROD_WARPS) {
     // ------------------------------------------------------------ producers
-    // Split each FP32 value of a raw chunk into TF32 hi and lo and store both tiles;
-    // every warp releases the raw stage on its own (raw_empty counts warps).
+    // Split each FP32 value of a raw chunk into hi and lo and store both tiles; every warp
+    // releases the raw stage on its own (raw_empty counts warps).
     const int BX = p.rbx, boxb = p.rbox_bytes;
     const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(BX - 1)) : 0;
     const int cofs = p.rnbox == 1 ? (cb & 15) - x0 : 0;
     const unsigned char *raw0 = smem + STAGES * STAGE_BYTES;
-    const int nq = p.CS / 2;        // channel pairs
-    const int ntask = 8 * n * nq;   // (16-byte chunk of 4 FFTs, stream, pair) per stage
+    const int nq = p.CS / 2;           // channel pairs
+    const int kq = KCR / TKC;          // 16-byte K chunks per raw chunk
+    const int ntask = kq * n * nq;     // (pair, stream, K chunk) per raw chunk
     const size_t tstride = (size_t)n * BX * 8;  // bytes between FFT rows of a box
-    for (int ch = 0; ch < nchunks; ch++) {
+    const float sc = p.split_sc;
+    bool ok = true;
+    for (int ch = 0; ch < nchunks && ok; ch++) {
       const int st = ch % STAGES;
-      const int rs = ch % RSTAGES;
       if (ch >= STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err)) break;
-      if (!mbar_wait(smem_u32(&raw_full[rs]), (ch / RSTAGES) & 1, p.err)) break;
       unsigned char *stage = smem + (size_t)st * STAGE_BYTES;
-      const unsigned char *raw = raw0 + rs * RAW_BYTES;
-      // task = (pair q, stream s, 16-byte K chunk o), q then s fastest across lanes: a
-      // warp reads consecutive 16-byte pieces of one FFT row (conflict-free), two
-      // tasks per thread in flight
-      for (int task0 = tid; task0 < ntask; task0 += 2 * NPROD) {
-        float4 v[2][4];
-#pragma unroll
-        for (int u2 = 0; u2 < 2; u2++) {
-          const int task = task0 + u2 * NPROD;
-          const int q = task % nq;
-          const int rest = task / nq;
-          const int s = rest % n;
-          const int o = rest / n;
-          const int cc0 = cofs + 2 * q;
-          const unsigned char *src = raw + (cc0 >> 4) * boxb + ((size_t)(4 * o) * n + s) * BX * 8 + (cc0 & 15) * 8;
-#pragma unroll
-          for (int i = 0; i < 4; i++)
-            v[u2][i] = task < ntask ? *reinterpret_cast<const float4 *>(src + i * tstride)
-                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int rr = 0; rr < RPO; rr++) {
+        const int rc = ch * RPO + rr;
+        const int rs = rc % RSTAGES;
+        if (!mbar_wait(smem_u32(&raw_full[rs]), (rc / RSTAGES) & 1, p.err)) {
+          ok = false;
+          break;
         }
+        const unsigned char *raw = raw0 + rs * RAW_BYTES;
+        // task = (pair q, stream s, 16-byte K chunk o), q then s fastest across lanes: a warp
+        // reads consecutive 16-byte pieces of one FFT row (conflict-free)
+        constexpr int UT = H16 ? 1 : 2;  // tasks per thread in flight (TKC float4 loads each)
+        for (int task0 = tid; task0 < ntask; task0 += UT * NPROD) {
+          float4 v[UT][TKC];
 #pragma unroll
-        for (int u2 = 0; u2 < 2; u2++) {
-          const int task = task0 + u2 * NPROD;
-          if (task >= ntask) break;
-          const int q = task % nq;
-          const int rest = task / nq;
-          const int s = rest % n;
-          const int o = rest / n;
-          // which part (re, im) this lane stores first: among 8 lanes the first stores
-          // then cover all 8 swizzle positions (no bank conflicts)
-          const int sw = nq == 1 ? ((s >> 2) & 1) : (q & 1);
+          for (int u2 = 0; u2 < UT; u2++) {
+            const int task = task0 + u2 * NPROD;
+            const int q = task % nq;
+            const int rest = task / nq;
+            const int s = rest % n;
+            const int o = rest / n;
+            const int cc0 = cofs + 2 * q;
+            const unsigned char *src =
+                raw + (cc0 >> 4) * boxb + ((size_t)(TKC * o) * n + s) * BX * 8 + (cc0 & 15) * 8;
 #pragma unroll
-          for (int ci = 0; ci < 2; ci++) {
-            const int cc = 2 * q + ci;
-            const int G = cc / GCH, gi = cc - G * GCH;
+            for (int i = 0; i < TKC; i++)
+              v[u2][i] = task < ntask ? *reinterpret_cast<const float4 *>(src + i * tstride)
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
 #pragma unroll
-            for (int pp = 0; pp < 2; pp++) {
-              const int part = pp ^ sw;
-              const int row = gi * R + 2 * s + part;
-              uint32_t hi[4], lo[4];
+          for (int u2 = 0; u2 < UT; u2++) {
+            const int task = task0 + u2 * NPROD;
+            if (task >= ntask) break;
+            const int q = task % nq;
+            const int rest = task / nq;
+            const int s = rest % n;
+            const int o = rest / n;
+            const int oo = rr * kq + o;  // K chunk within the 128-byte row
+            // which part (re, im) this lane stores first: among 8 lanes the first stores
+            // then cover all 8 swizzle positions (no bank conflicts)
+            const int sw = nq == 1 ? ((s >> 2) & 1) : (q & 1);
 #pragma unroll
-              for (int i = 0; i < 4; i++) {
-                const float4 &f = v[u2][i];
-                const float x = ci ? (part ? f.w : f.z) : (part ? f.y : f.x);
-                hi[i] = __float_as_uint(x) & 0xFFFFE000u;
-                lo[i] = __float_as_uint(x - __uint_as_float(hi[i]));
+            for (int ci = 0; ci < 2; ci++) {
+              const int cc = 2 * q + ci;
+              const int G = cc / GCH, gi = cc - G * GCH;
+#pragma unroll
+              for (int pp = 0; pp < 2; pp++) {
+                const int part = pp ^ sw;
+                const int row = gi * R + 2 * s + part;
+                uint32_t hi[4], lo[4];
+                if constexpr (H16) {
+#pragma unroll
+                  for (int i = 0; i < 4; i++) {
+                    const float4 &f0 = v[u2][2 * i], &f1 = v[u2][2 * i + 1];
+                    const float x0v = sc * (ci ? (part ? f0.w : f0.z) : (part ? f0.y : f0.x));
+                    const float x1v = sc * (ci ? (part ? f1.w : f1.z) : (part ? f1.y : f1.x));
+                    const __half h0 = __float2half_rn(x0v), h1 = __float2half_rn(x1v);
+                    const __half l0 = __float2half_rn(x0v - __half2float(h0));
+                    const __half l1 = __float2half_rn(x1v - __half2float(h1));
+                    hi[i] = (uint32_t)__half_as_ushort(h0) | ((uint32_t)__half_as_ushort(h1) << 16);
+                    lo[i] = (uint32_t)__half_as_ushort(l0) | ((uint32_t)__half_as_ushort(l1) << 16);
+                  }
+                } else {
+#pragma unroll
+                  for (int i = 0; i < 4; i++) {
+                    const float4 &f = v[u2][i];
+                    const float x = ci ? (part ? f.w : f.z) : (part ? f.y : f.x);
+                    hi[i] = __float_as_uint(x) & 0xFFFFE000u;
+                    lo[i] = __float_as_uint(x - __uint_as_float(hi[i]));
+                  }
+                }
+                unsigned char *gbase = stage + G * GROUP_BYTES;
+                const int swz = (oo ^ (row & 7)) << 4;
+                *reinterpret_cast<uint4 *>(gbase + row * 128 + swz) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                *reinterpret_cast<uint4 *>(gbase + TILE_BYTES + row * 128 + swz) =
+                    make_uint4(lo[0], lo[1], lo[2], lo[3]);
               }
-              unsigned char *gbase = stage + G * GROUP_BYTES;
-              const int swz = (o ^ (row & 7)) << 4;
-              *reinterpret_cast<uint4 *>(gbase + row * 128 + swz) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-              *reinterpret_cast<uint4 *>(gbase + TILE_BYTES + row * 128 + swz) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
             }
           }
         }
+        __syncwarp();  // this warp's reads of the raw stage are done (their values are stored)
+        if (lane == 0) mbar_arrive(smem_u32(&raw_empty[rs]));
       }
-      __syncwarp();  // this warp's reads of the raw stage are done (their values are stored)
-      if (lane == 0) mbar_arrive(smem_u32(&raw_empty[rs]));
+      if (!ok) break;
       fence_proxy_async_smem();
       mbar_arrive(smem_u32(&bar_full[st]));
     }
@@ -707,12 +747,18 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
         for (int G = 0; G < NG; G++) {
           const uint32_t d = tmem + b * SET_COLS + G * 128;
 #pragma unroll
-          for (int kk = 0; kk < KC / C::KSTEP; kk++) {
+          for (int kk = 0; kk < KC / KSTEP; kk++) {
             const uint64_t dh = desc_sw128(sa + G * GROUP_BYTES + kk * 32);
             const uint64_t dl = desc_sw128(sa + G * GROUP_BYTES + TILE_BYTES + kk * 32);
-            mma_tf32(d, dh, dh, IDESC_TF32, (first && kk == 0) ? 0u : 1u);
-            mma_tf32(d, dl, dh, IDESC_TF32, 1u);
-            mma_tf32(d, dh, dl, IDESC_TF32, 1u);
+            if constexpr (H16) {
+              mma_f16(d, dh, dh, IDESC, (first && kk == 0) ? 0u : 1u);
+              mma_f16(d, dl, dh, IDESC, 1u);
+              mma_f16(d, dh, dl, IDESC, 1u);
+            } else {
+              mma_tf32(d, dh, dh, IDESC_TF32, (first && kk == 0) ? 0u : 1u);
+              mma_tf32(d, dl, dh, IDESC_TF32, 1u);
+              mma_tf32(d, dh, dl, IDESC_TF32, 1u);
+            }
           }
         }
         mma_commit(smem_u32(&bar_empty[st]));
@@ -796,8 +842,8 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
             const int bl = baseline_index(j, k, p.nant);
             const size_t o = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
             float2 sm = p.vsum[o], e = p.vcomp[o];
-            two_sum_add(sm.x, e.x, acc[G][a][qq].x);
-            two_sum_add(sm.y, e.y, acc[G][a][qq].y);
+            two_sum_add(sm.x, e.x, acc[G][a][qq].x * p.split_unsc);  // exact: a power of two
+            two_sum_add(sm.y, e.y, acc[G][a][qq].y * p.split_unsc);
             p.vsum[o] = sm;
             p.vcomp[o] = e;
           }
@@ -1331,7 +1377,7 @@ int xstage_tensor_fits(int nant, int nchan, int chan_type) {
 }
 
 cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,
-                                 float2 *vsum, float2 *vcomp, cudaStream_t s) {
+                                 float2 *vsum, float2 *vcomp, cudaStream_t s, int split_e) {
   if (nt <= 0) return cudaSuccess;
   if (!xstage_tensor_supported(nant)) return cudaErrorInvalidValue;
   tc::Params p;
@@ -1350,6 +1396,10 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   if (p.CS <= 0 || nchan % p.CS) return cudaErrorInvalidValue;
   p.vsum = vsum;
   p.vcomp = vcomp;
+  // FP32 data: FP16 hi/lo split of values scaled by 2^-split_e when split_e >= 0, else TF32 split
+  const bool h16 = chan_type == CHAN_F32 && split_e >= 0;
+  p.split_sc = h16 ? ldexpf(1.0f, -split_e) : 1.0f;
+  p.split_unsc = h16 ? ldexpf(1.0f, 2 * split_e) : 1.0f;
   cudaError_t e = xstage_tensor_error_flag(&p.err);
   if (e != cudaSuccess) return e;
   if (R > 128) {
@@ -1372,7 +1422,7 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   // small-N kernels: raw TMA tiles of rbx channels (at least 16 bytes: FP8 with 4 channels per
   // CTA loads 8, of which the CTA uses its 4) x all streams x rkc FFTs, one box per channel tile
   const int esz = (int)chan_elem_bytes(chan_type);
-  const int KC = chan_type == CHAN_F32 ? tc::Cfg<true>::KC : chan_type == CHAN_F8 ? 128 : tc::Cfg<false>::KC;
+  const int KC = chan_type == CHAN_F32 ? (h16 ? 64 : tc::Cfg<true>::KC) : chan_type == CHAN_F8 ? 128 : tc::Cfg<false>::KC;
   p.rnbox = p.CS > CW ? p.CS / CW : 1;
   p.rbx = p.CS > CW ? CW : (p.CS * esz >= 16 ? p.CS : 16 / esz);
   if (p.rbx * esz < 16 || p.rbx > CW || (p.CS > CW && p.CS % CW)) return cudaErrorInvalidValue;
@@ -1380,7 +1430,7 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   while (kc > 8 && (size_t)p.rnbox * p.rbx * p.nstream * kc * esz > (size_t)tc::RAW_BYTES) kc >>= 1;
   p.rkc = kc;
   p.rbox_bytes = p.rbx * p.nstream * kc * esz;
-  if ((size_t)p.rnbox * p.rbox_bytes > (size_t)tc::RAW_BYTES || KC % kc || (chan_type == CHAN_F32 && kc != KC) ||
+  if ((size_t)p.rnbox * p.rbox_bytes > (size_t)tc::RAW_BYTES || KC % kc ||
       kc % (chan_type == CHAN_F8 ? 16 : 8))
     return cudaErrorInvalidValue;
   CUtensorMap tmap;
@@ -1395,11 +1445,15 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
       kern<<<nchan / p.CS, tc::NTHREADS_SPLIT, smem, s>>>(p, tmap);
       return cudaSuccess;
     };
-    switch (R) {
-      case 16: e = launch(tc::xstage_tc_split_kernel<16>); break;
-      case 32: e = launch(tc::xstage_tc_split_kernel<32>); break;
-      case 64: e = launch(tc::xstage_tc_split_kernel<64>); break;
-      case 128: e = launch(tc::xstage_tc_split_kernel<128>); break;
+    switch (R * 2 + (h16 ? 1 : 0)) {
+      case 32: e = launch(tc::xstage_tc_split_kernel<16, false>); break;
+      case 33: e = launch(tc::xstage_tc_split_kernel<16, true>); break;
+      case 64: e = launch(tc::xstage_tc_split_kernel<32, false>); break;
+      case 65: e = launch(tc::xstage_tc_split_kernel<32, true>); break;
+      case 128: e = launch(tc::xstage_tc_split_kernel<64, false>); break;
+      case 129: e = launch(tc::xstage_tc_split_kernel<64, true>); break;
+      case 256: e = launch(tc::xstage_tc_split_kernel<128, false>); break;
+      case 257: e = launch(tc::xstage_tc_split_kernel<128, true>); break;
       default: return cudaErrorInvalidValue;
     }
     if (e != cudaSuccess) return e;
