@@ -130,24 +130,66 @@ cudaError_t launch_counts(const Job &job, int autos, int32_t *counts, uint8_t *v
 }
 
 // ----------------------------------------------------------------- twiddles
-// tw[m] = exp(-2 pi i m / F), m < F, rounded once from double.
+// Number of float4 pass-twiddle entries that follow the F-point table when F = 8192.
+constexpr int kPairTw = 16 * 16 + 16 * 256;
+
+// tw[m] = exp(-2 pi i m / F), m < F, rounded once from double.  For F = 8192 the same
+// allocation continues with the pass twiddles of the packed-pair kernel as broadcast pairs
+// {c, c, s, s} of W_M^e, M = F/2, laid out so that a warp reads consecutive entries:
+//   [r][k]  (256 entries):  e = 16 r k,  k < 16  (pass 1)
+//   [r][iv] (4096 entries): e = r iv,    iv < 256 (pass 2)
 cudaError_t make_twiddles(int F, float2 **out) {
-  std::vector<float2> h((size_t)F);
+  const size_t extra = F == 8192 ? 2 * (size_t)kPairTw : 0;  // float4 = two float2
+  std::vector<float2> h((size_t)F + extra);
   for (int m = 0; m < F; m++) {
     const double ang = -2.0 * 3.14159265358979323846 * (double)m / (double)F;
     h[(size_t)m] = make_float2((float)cos(ang), (float)sin(ang));
   }
-  cudaError_t e = cudaMalloc((void **)out, sizeof(float2) * (size_t)F);
+  if (extra) {
+    auto put = [&](size_t slot, int e) {  // W_M^e = tw[2e mod F]
+      const float2 w = h[(size_t)((2 * (long long)e) % F)];
+      h[(size_t)F + 2 * slot] = make_float2(w.x, w.x);
+      h[(size_t)F + 2 * slot + 1] = make_float2(w.y, w.y);
+    };
+    for (int r = 0; r < 16; r++)
+      for (int k = 0; k < 16; k++) put((size_t)r * 16 + k, 16 * r * k);
+    for (int r = 0; r < 16; r++)
+      for (int iv = 0; iv < 256; iv++) put(256 + (size_t)r * 256 + iv, r * iv);
+  }
+  cudaError_t e = cudaMalloc((void **)out, sizeof(float2) * h.size());
   if (e != cudaSuccess) return e;
-  return cudaMemcpy(*out, h.data(), sizeof(float2) * (size_t)F, cudaMemcpyHostToDevice);
+  return cudaMemcpy(*out, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice);
 }
 
 // ------------------------------------------------------------ FFT helpers
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add and subtract as one packed FP32-pair instruction each (add/sub.rn.f32x2,
+// sm_100 and later): IEEE round-to-nearest per component, as the scalar adds, in half
+// the issue slots.
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  float2 r;
+  asm("{.reg .b64 pa, pb, pd;\n\t"
+      "mov.b64 pa, {%2, %3};\n\t"
+      "mov.b64 pb, {%4, %5};\n\t"
+      "add.rn.f32x2 pd, pa, pb;\n\t"
+      "mov.b64 {%0, %1}, pd;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  float2 r;
+  asm("{.reg .b64 pa, pb, pd;\n\t"
+      "mov.b64 pa, {%2, %3};\n\t"
+      "mov.b64 pb, {%4, %5};\n\t"
+      "sub.rn.f32x2 pd, pa, pb;\n\t"
+      "mov.b64 {%0, %1}, pd;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
 // -i * a
 __device__ __forceinline__ float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }
 
@@ -237,7 +279,8 @@ template <> __device__ __forceinline__ __nv_fp8x2_e4m3 to_out<__nv_fp8x2_e4m3>(f
 
 struct FParams {
   Job job;
-  const float2 *tw;
+  const float2 *tw;    // W_F^m, m < F
+  const float4 *twq;   // F = 8192: pass twiddles of the packed-pair kernel (make_twiddles), else null
   int t0, T;
   void *chan;
   float out_scale;
@@ -505,6 +548,318 @@ __global__ void __launch_bounds__(FPlan<L, CPLX>::NT, FPlan<L, CPLX>::MINB) fsta
       }
     }
   }
+}
+
+// -------------------------------------- 8192-point windows in packed FP32 pairs
+// One radix-2 decimation-in-frequency step splits the N-point FFT into two
+// M = N/2-point FFTs with the same structure and the same twiddles:
+//   A[k] = X[2k]   = DFT_M( x[n] + x[n+M] )
+//   B[k] = X[2k+1] = DFT_M( (x[n] - x[n+M]) W_N^n ),   n < M.
+// A and B travel as the two lanes of packed FP32-pair registers, re = (A.re, B.re)
+// and im = (A.im, B.im), so every add, subtract and twiddle multiply of both
+// sub-FFTs is one packed instruction (add/sub/mul/fma.rn.f32x2: IEEE round to
+// nearest per lane, half the issue slots of scalar code).  The sub-FFTs use the
+// radix 16 x 16 x 16 Stockham schedule of the 4096-point kernel; bins 2k and
+// 2k+1 are neighbouring channels and leave in one vector store.
+
+struct P2 {
+  float2 re, im;  // (A, B) lanes
+};
+
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) {
+  float2 r;
+  asm("{.reg .b64 pa, pb, pd;\n\t"
+      "mov.b64 pa, {%2, %3};\n\t"
+      "mov.b64 pb, {%4, %5};\n\t"
+      "mul.rn.f32x2 pd, pa, pb;\n\t"
+      "mov.b64 {%0, %1}, pd;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+// a * b + c per lane, one rounding
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) {
+  float2 r;
+  asm("{.reg .b64 pa, pb, pc, pd;\n\t"
+      "mov.b64 pa, {%2, %3};\n\t"
+      "mov.b64 pb, {%4, %5};\n\t"
+      "mov.b64 pc, {%6, %7};\n\t"
+      "fma.rn.f32x2 pd, pa, pb, pc;\n\t"
+      "mov.b64 {%0, %1}, pd;}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return r;
+}
+// both lanes times w, given as the broadcast pairs WR = (w.re, w.re), WI = (w.im, w.im)
+__device__ __forceinline__ void pcmul(P2 &u, float2 WR, float2 WI) {
+  const float2 re = csub(pmul(u.re, WR), pmul(u.im, WI));
+  u.im = pfma(u.re, WI, pmul(u.im, WR));
+  u.re = re;
+}
+// both lanes times the constant (cr, ci)
+__device__ __forceinline__ void pcmul_c(P2 &u, float cr, float ci) {
+  const float2 CR = make_float2(cr, cr), CI = make_float2(ci, ci), NCI = make_float2(-ci, -ci);
+  const float2 re = pfma(u.re, CR, pmul(u.im, NCI));
+  u.im = pfma(u.re, CI, pmul(u.im, CR));
+  u.re = re;
+}
+
+// 4-point DFT of both lanes.  X2MI: the x2 operand holds z with x2 = -i z (the W16^4
+// twiddle folded in).  KEEP2: only X0 and X1 are needed.
+template <bool X2MI, bool KEEP2>
+__device__ __forceinline__ void dft4p(P2 &x0, P2 &x1, P2 &x2, P2 &x3) {
+  float2 s02r, s02i, d02r, d02i;
+  if constexpr (X2MI) {  // x2 = (z.im, -z.re)
+    s02r = cadd(x0.re, x2.im);
+    s02i = csub(x0.im, x2.re);
+    d02r = csub(x0.re, x2.im);
+    d02i = cadd(x0.im, x2.re);
+  } else {
+    s02r = cadd(x0.re, x2.re);
+    s02i = cadd(x0.im, x2.im);
+    d02r = csub(x0.re, x2.re);
+    d02i = csub(x0.im, x2.im);
+  }
+  const float2 s13r = cadd(x1.re, x3.re), s13i = cadd(x1.im, x3.im);
+  const float2 tr = csub(x1.re, x3.re), ti = csub(x1.im, x3.im);
+  x0.re = cadd(s02r, s13r);
+  x0.im = cadd(s02i, s13i);
+  // X1 = d02 - i t, X3 = d02 + i t
+  x1.re = cadd(d02r, ti);
+  x1.im = csub(d02i, tr);
+  if constexpr (!KEEP2) {
+    x2.re = csub(s02r, s13r);
+    x2.im = csub(s02i, s13i);
+    x3.re = csub(d02r, ti);
+    x3.im = cadd(d02i, tr);
+  }
+}
+
+// 16-point DFT of both lanes, the 4 x 4 factorisation of dft<16>.  KEEP8: only
+// outputs k < 8 are needed (real data keeps the lower half of the band).
+template <bool KEEP8>
+__device__ __forceinline__ void dft16p(P2 *u) {
+  const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f, r = 0.70710678118654752440f;
+#pragma unroll
+  for (int n2 = 0; n2 < 4; n2++) dft4p<false, false>(u[n2], u[n2 + 4], u[n2 + 8], u[n2 + 12]);
+  // u[n2 + 4 k1] = Y[n2][k1]; twiddle by W16^(n2 k1) (W^4 = -i is folded into the k1 = 2 DFT)
+  pcmul_c(u[5], c1, -s1);
+  pcmul_c(u[9], r, -r);
+  pcmul_c(u[13], s1, -c1);
+  pcmul_c(u[6], r, -r);
+  pcmul_c(u[14], -r, -r);
+  pcmul_c(u[7], s1, -c1);
+  pcmul_c(u[11], -r, -r);
+  pcmul_c(u[15], -c1, s1);
+  P2 y[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    P2 a = u[4 * k1], b = u[4 * k1 + 1], c = u[4 * k1 + 2], d = u[4 * k1 + 3];
+    if (k1 == 2) dft4p<true, KEEP8>(a, b, c, d);
+    else dft4p<false, KEEP8>(a, b, c, d);
+    y[k1] = a;
+    y[k1 + 4] = b;
+    y[k1 + 8] = c;
+    y[k1 + 12] = d;
+  }
+#pragma unroll
+  for (int q = 0; q < 16; q++) u[q] = y[q];
+}
+
+// channels c and c+1 (c even) of one stream: one 16-, 8- or 4-byte store
+template <typename OutT> __device__ __forceinline__ void store_pair(OutT *p, float2 a, float2 b);
+template <> __device__ __forceinline__ void store_pair<float2>(float2 *p, float2 a, float2 b) {
+  *reinterpret_cast<float4 *>(p) = make_float4(a.x, a.y, b.x, b.y);
+}
+template <> __device__ __forceinline__ void store_pair<__half2>(__half2 *p, float2 a, float2 b) {
+  const __half2 ha = __floats2half2_rn(a.x, a.y), hb = __floats2half2_rn(b.x, b.y);
+  *reinterpret_cast<uint2 *>(p) =
+      make_uint2(*reinterpret_cast<const uint32_t *>(&ha), *reinterpret_cast<const uint32_t *>(&hb));
+}
+template <>
+__device__ __forceinline__ void store_pair<__nv_fp8x2_e4m3>(__nv_fp8x2_e4m3 *p, float2 a, float2 b) {
+  const __nv_fp8x2_e4m3 ea(a), eb(b);
+  *reinterpret_cast<uint32_t *>(p) = (uint32_t)ea.__x | ((uint32_t)eb.__x << 16);
+}
+
+template <typename OutT, bool CPLX>
+__global__ void __launch_bounds__(256, 2) fstage_pair_kernel(FParams prm) {
+  using Pl = FPlan<13, CPLX>;  // window, rotator and frac-delay tables of the 8192-point FFT
+  constexpr int N = Pl::N, M = N / 2, NT = 256, R = 16, PAD = 16;
+  constexpr int NB = M / R;         // 256: butterflies per radix-16 pass (one per thread)
+  constexpr int NB0 = N / 32;       // 256: pass 0 takes the samples n = iv + r*NB0, r < 32
+  constexpr int PADM = M + M / PAD;
+  constexpr int SUB = Pl::SUB, STRIDE = Pl::STRIDE, FSUB = Pl::FSUB, NCHAN = Pl::NCHAN;
+  static_assert(NB == NT && NB0 % SUB == 0 && (2 * NB) % FSUB == 0 && NB % PAD == 0, "pair plan");
+  const Job &job = prm.job;
+  extern __shared__ float4 smem4[];
+  float4 *buf = smem4;  // [PADM] pair elements {A.re, B.re, A.im, B.im}
+  float2 *tsub = reinterpret_cast<float2 *>(buf + PADM);
+  float2 *tstep = tsub + SUB;
+  float2 *fsubt = tstep + STRIDE;
+  float2 *fstept = fsubt + FSUB;
+  unsigned char *stage = reinterpret_cast<unsigned char *>(fstept + STRIDE);
+
+  const int pol = blockIdx.x & 1;
+  const int tl = blockIdx.x >> 1;
+  const int ant = blockIdx.y;
+  const int t = prm.t0 + tl;
+  const int iv = threadIdx.x;
+  const int nstreams = 2 * job.nant;
+  const int s = 2 * ant + pol;
+  OutT *chan = reinterpret_cast<OutT *>(prm.chan);
+  const Geom g = job.geom[(size_t)ant * job.nfft + t];
+  OutT *out0 = chan + ((size_t)tl * nstreams + s) * CW;
+  const size_t ctile_stride = (size_t)prm.T * nstreams * CW;
+
+  if (!g.valid) {
+    const OutT z = to_out<OutT>(make_float2(0.f, 0.f), 1.f);
+    for (int c = iv; c < NCHAN; c += NT) out0[(size_t)(c >> 4) * ctile_stride + (c & 15)] = z;
+    return;
+  }
+
+  const long long stage_base = (CPLX ? 4LL * g.offset : ((long long)g.offset >> 1)) & ~15LL;
+  {
+    // the packed window, 16-byte asynchronous copies (the buffer holds (nfft+1)*F samples and
+    // offset <= (nfft-1)*F, so the window plus the 16-byte rounding stays inside it); the
+    // rotator and frac-delay tables are evaluated while the copies are in flight
+    const uint4 *src = reinterpret_cast<const uint4 *>(job.inputs[ant] + stage_base);
+    const long long last = CPLX ? 4LL * (g.offset + N) : (((long long)g.offset + N + 1) >> 1);
+    const int nvec = (int)((last - stage_base + 15) >> 4);
+    uint4 *dst = reinterpret_cast<uint4 *>(stage);
+    for (int i = iv; i < nvec; i += NT) cp_async16(dst + i, src + i);
+    const float c0 = g.c0, c1 = g.c1, cstep = g.cstep, cf = g.cf;
+    for (int k = iv; k < SUB; k += NT) {
+      float sn, cs;
+      sincospif(-2.0f * fmaf((float)k, c1, c0), &sn, &cs);
+      tsub[k] = make_float2(cs, sn);
+    }
+    for (int i = iv; i < STRIDE; i += NT) {
+      float sn, cs;
+      sincospif(-2.0f * ((float)i * cstep), &sn, &cs);
+      tstep[i] = make_float2(cs, sn);
+      sincospif(2.0f * ((float)(i * FSUB) * cf), &sn, &cs);
+      fstept[i] = make_float2(cs, sn);
+    }
+    for (int k = iv; k < FSUB; k += NT) {
+      float sn, cs;
+      sincospif(2.0f * ((float)k * cf), &sn, &cs);
+      fsubt[k] = make_float2(cs, sn);
+    }
+    cp_async_wait_all();
+  }
+  __syncthreads();
+
+  P2 u[R];
+  // ---- pass 0: decode + fringe-rotate x[n] and x[n+M], n = iv + r*NB0 (r < 16), form the
+  //      lanes A = x[n] + x[n+M], B = (x[n] - x[n+M]) W_N^n, then radix 16 over r
+  {
+    const int off = g.offset;
+    const int sbase = (int)(CPLX ? (4LL * off - stage_base) : (((long long)off >> 1) - stage_base));
+    const float2 rs = tsub[iv & (SUB - 1)];
+    const int p0 = (off & 1) + iv;
+    const int shift = 2 * (2 * (p0 & 1) + pol);
+    auto sample = [&](int r) -> float2 {
+      const float2 rot = cmul(rs, tstep[(iv / SUB) + r * (NB0 / SUB)]);
+      if constexpr (CPLX) {
+        const char2 x = *reinterpret_cast<const char2 *>(stage + sbase + 4 * iv + 2 * pol + r * (4 * NB0));
+        return cmul(make_float2((float)x.x, (float)x.y), rot);
+      } else {
+        const int byte = stage[sbase + (p0 >> 1) + r * (NB0 / 2)];
+        const float lv = level2bit((byte >> shift) & 3);
+        return make_float2(lv * rot.x, lv * rot.y);
+      }
+    };
+    const float2 wiv = __ldg(&prm.tw[iv]);  // W_N^n = W_N^iv W_32^r
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float2 x0 = sample(r), x1 = sample(r + R);
+      const float2 w = cmul(wiv, make_float2(kC32[r], -kS32[r]));
+      const float2 b = cmul(make_float2(x0.x - x1.x, x0.y - x1.y), w);
+      u[r].re = make_float2(x0.x + x1.x, b.x);
+      u[r].im = make_float2(x0.y + x1.y, b.y);
+    }
+    dft16p<false>(u);
+    float4 *bp = buf + iv * (R + 1);
+#pragma unroll
+    for (int r = 0; r < R; r++) bp[r] = make_float4(u[r].re.x, u[r].re.y, u[r].im.x, u[r].im.y);
+  }
+  __syncthreads();
+  // ---- pass 1: radix 16, span 16 (in place)
+  {
+    const float4 *bp = buf + iv + iv / PAD;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float4 v = bp[r * (NB + NB / PAD)];
+      u[r].re = make_float2(v.x, v.y);
+      u[r].im = make_float2(v.z, v.w);
+    }
+    const int k = iv & (R - 1);
+#pragma unroll
+    for (int r = 1; r < R; r++) {  // W_M^(16 r k)
+      const float4 w = __ldg(&prm.twq[16 * r + k]);
+      pcmul(u[r], make_float2(w.x, w.y), make_float2(w.z, w.w));
+    }
+    dft16p<false>(u);
+  }
+  __syncthreads();
+  {
+    const int k = iv & (R - 1);
+    const int j = (iv - k) * R + k;
+    float4 *bp = buf + j + j / PAD;
+#pragma unroll
+    for (int r = 0; r < R; r++) bp[r * (R + R / PAD)] = make_float4(u[r].re.x, u[r].re.y, u[r].im.x, u[r].im.y);
+  }
+  __syncthreads();
+  // ---- pass 2: radix 16, span 256; sub-FFT bin kk = iv + r*NB is channel 2 kk (A) and 2 kk + 1 (B)
+  {
+    const float4 *bp = buf + iv + iv / PAD;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float4 v = bp[r * (NB + NB / PAD)];
+      u[r].re = make_float2(v.x, v.y);
+      u[r].im = make_float2(v.z, v.w);
+    }
+#pragma unroll
+    for (int r = 1; r < R; r++) {  // W_M^(r iv)
+      const float4 w = __ldg(&prm.twq[16 * 16 + NB * r + iv]);
+      pcmul(u[r], make_float2(w.x, w.y), make_float2(w.z, w.w));
+    }
+    dft16p<!CPLX>(u);
+    constexpr int RKEEP = CPLX ? R : R / 2;  // real data keeps channels c < N/2
+    // frac-delay: fine part fixed per thread (FSUB divides 2*NB), output scale (a power of two) folded in
+    const float sc = prm.out_scale;
+    const float2 fa = fsubt[(2 * iv) & (FSUB - 1)], fb = fsubt[(2 * iv + 1) & (FSUB - 1)];
+    const float2 fsA = make_float2(fa.x * sc, fa.y * sc), fsB = make_float2(fb.x * sc, fb.y * sc);
+    OutT *o = out0 + (size_t)((2 * iv) >> 4) * ctile_stride + ((2 * iv) & 15);
+#pragma unroll
+    for (int r = 0; r < RKEEP; r++) {
+      const float2 fst = fstept[(2 * iv) / FSUB + r * (2 * NB / FSUB)];
+      const float2 a = cmul(make_float2(u[r].re.x, u[r].im.x), cmul(fsA, fst));
+      const float2 b = cmul(make_float2(u[r].re.y, u[r].im.y), cmul(fsB, fst));
+      store_pair<OutT>(o + (size_t)r * (2 * NB / 16) * ctile_stride, a, b);
+    }
+  }
+}
+
+template <typename OutT, bool CPLX>
+static cudaError_t launch_fstage_pair(const FParams &prm, int nt, cudaStream_t s) {
+  using Pl = FPlan<13, CPLX>;
+  const Job &job = prm.job;
+  if (job.substride != Pl::SUB || job.stride != Pl::STRIDE || job.fsub != Pl::FSUB || job.fstride != Pl::STRIDE ||
+      job.nchan != Pl::NCHAN)
+    return cudaErrorInvalidValue;
+  constexpr int M = Pl::N / 2;
+  const size_t stage_bytes = CPLX ? 4 * (size_t)Pl::N + 32 : (size_t)Pl::N / 2 + 32;
+  const size_t smem = sizeof(float4) * ((size_t)M + M / 16) +
+                      sizeof(float2) * ((size_t)Pl::SUB + 2 * Pl::STRIDE + Pl::FSUB) +
+                      ((stage_bytes + 15) & ~(size_t)15);
+  auto kern = fstage_pair_kernel<OutT, CPLX>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid(2u * (unsigned)nt, (unsigned)job.nant, 1u);
+  kern<<<grid, 256, smem, s>>>(prm);
+  return cudaGetLastError();
 }
 
 template <int L, typename OutT, bool CPLX>
@@ -953,7 +1308,7 @@ static cudaError_t launch_fstage_l(const FParams &prm, int nt, cudaStream_t s) {
     case 10: return launch_fstage_t<10, OutT, CPLX>(prm, nt, s);
     case 11: return launch_fstage_t<11, OutT, CPLX>(prm, nt, s);
     case 12: return launch_fstage_t<12, OutT, CPLX>(prm, nt, s);
-    case 13: return launch_fstage_t<13, OutT, CPLX>(prm, nt, s);
+    case 13: return launch_fstage_pair<OutT, CPLX>(prm, nt, s);  // packed FP32 pairs
     case 14:  // FP32 output: FP32 shared buffer; FP16 / FP8 output: FP16 buffer, two CTAs per SM
       if constexpr (std::is_same<OutT, float2>::value) return launch_fstage_t<14, OutT, CPLX>(prm, nt, s);
       else return launch_fstage_h<14, OutT, CPLX>(prm, nt, s);
@@ -978,6 +1333,7 @@ cudaError_t launch_fstage(const Job &job, const float2 *twiddles, int t0, int nt
   FParams prm;
   prm.job = job;
   prm.tw = twiddles;
+  prm.twq = job.F == 8192 ? reinterpret_cast<const float4 *>(twiddles + job.F) : nullptr;
   prm.t0 = t0;
   prm.T = T;
   prm.chan = chan;
