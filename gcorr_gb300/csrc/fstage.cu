@@ -130,31 +130,32 @@ cudaError_t launch_counts(const Job &job, int autos, int32_t *counts, uint8_t *v
 }
 
 // ----------------------------------------------------------------- twiddles
-// Number of float4 pass-twiddle entries that follow the F-point table when F = 8192.
-constexpr int kPairTw = 16 * 16 + 16 * 256;
+// float2 slots that follow the F-point table when F = 8192: 256 float4 + 4096 float2.
+constexpr int kPairTw1 = 16 * 16, kPairTw2 = 16 * 256;
 
 // tw[m] = exp(-2 pi i m / F), m < F, rounded once from double.  For F = 8192 the same
-// allocation continues with the pass twiddles of the packed-pair kernel as broadcast pairs
-// {c, c, s, s} of W_M^e, M = F/2, laid out so that a warp reads consecutive entries:
-//   [r][k]  (256 entries):  e = 16 r k,  k < 16  (pass 1)
-//   [r][iv] (4096 entries): e = r iv,    iv < 256 (pass 2)
+// allocation continues with the pass twiddles W_M^e (M = F/2) of the packed-pair kernel,
+// laid out so that a warp reads consecutive entries:
+//   pass 1, [r][k]  (256 float4 broadcast pairs {c, c, s, s}): e = 16 r k, k < 16
+//   pass 2, [r][iv] (4096 float2 {c, s}, half the L1 footprint): e = r iv, iv < 256
 cudaError_t make_twiddles(int F, float2 **out) {
-  const size_t extra = F == 8192 ? 2 * (size_t)kPairTw : 0;  // float4 = two float2
+  const size_t extra = F == 8192 ? 2 * (size_t)kPairTw1 + kPairTw2 : 0;
   std::vector<float2> h((size_t)F + extra);
   for (int m = 0; m < F; m++) {
     const double ang = -2.0 * 3.14159265358979323846 * (double)m / (double)F;
     h[(size_t)m] = make_float2((float)cos(ang), (float)sin(ang));
   }
   if (extra) {
-    auto put = [&](size_t slot, int e) {  // W_M^e = tw[2e mod F]
-      const float2 w = h[(size_t)((2 * (long long)e) % F)];
-      h[(size_t)F + 2 * slot] = make_float2(w.x, w.x);
-      h[(size_t)F + 2 * slot + 1] = make_float2(w.y, w.y);
-    };
+    auto wm = [&](int e) { return h[(size_t)((2 * (long long)e) % F)]; };  // W_M^e = W_F^(2e)
     for (int r = 0; r < 16; r++)
-      for (int k = 0; k < 16; k++) put((size_t)r * 16 + k, 16 * r * k);
+      for (int k = 0; k < 16; k++) {
+        const float2 w = wm(16 * r * k);
+        const size_t slot = (size_t)F + 2 * ((size_t)r * 16 + k);
+        h[slot] = make_float2(w.x, w.x);
+        h[slot + 1] = make_float2(w.y, w.y);
+      }
     for (int r = 0; r < 16; r++)
-      for (int iv = 0; iv < 256; iv++) put(256 + (size_t)r * 256 + iv, r * iv);
+      for (int iv = 0; iv < 256; iv++) h[(size_t)F + 2 * kPairTw1 + (size_t)r * 256 + iv] = wm(r * iv);
   }
   cudaError_t e = cudaMalloc((void **)out, sizeof(float2) * h.size());
   if (e != cudaSuccess) return e;
@@ -280,7 +281,8 @@ template <> __device__ __forceinline__ __nv_fp8x2_e4m3 to_out<__nv_fp8x2_e4m3>(f
 struct FParams {
   Job job;
   const float2 *tw;    // W_F^m, m < F
-  const float4 *twq;   // F = 8192: pass twiddles of the packed-pair kernel (make_twiddles), else null
+  const float4 *twq;   // F = 8192: pass-1 twiddles of the packed-pair kernel (make_twiddles), else null
+  const float2 *twp2;  // F = 8192: pass-2 twiddles of the packed-pair kernel, else null
   int t0, T;
   void *chan;
   float out_scale;
@@ -822,8 +824,8 @@ __global__ void __launch_bounds__(256, 2) fstage_pair_kernel(FParams prm) {
     }
 #pragma unroll
     for (int r = 1; r < R; r++) {  // W_M^(r iv)
-      const float4 w = __ldg(&prm.twq[16 * 16 + NB * r + iv]);
-      pcmul(u[r], make_float2(w.x, w.y), make_float2(w.z, w.w));
+      const float2 w = __ldg(&prm.twp2[NB * r + iv]);
+      pcmul(u[r], make_float2(w.x, w.x), make_float2(w.y, w.y));
     }
     dft16p<!CPLX>(u);
     constexpr int RKEEP = CPLX ? R : R / 2;  // real data keeps channels c < N/2
@@ -1334,6 +1336,7 @@ cudaError_t launch_fstage(const Job &job, const float2 *twiddles, int t0, int nt
   prm.job = job;
   prm.tw = twiddles;
   prm.twq = job.F == 8192 ? reinterpret_cast<const float4 *>(twiddles + job.F) : nullptr;
+  prm.twp2 = job.F == 8192 ? twiddles + job.F + 2 * kPairTw1 : nullptr;
   prm.t0 = t0;
   prm.T = T;
   prm.chan = chan;
