@@ -534,8 +534,17 @@ def main():
         t = tdata.get(key)
         return None if not t else t["per_fft"] * ffts_per_launch + t.get("per_launch_const", 0)
 
+    # the F-stage kernel this FFT length and precision runs
+    if w.fft_len == 8192:
+        fkern = "fstage_pair_kernel"
+    elif w.fft_len >= 16384 and args.precision != "fp32":
+        fkern = "fstage_h_kernel"
+    elif w.fft_len == 32768:
+        fkern = "fstage_cluster_kernel"
+    else:
+        fkern = "fstage_kernel"
     if f_ms >= x_ms:
-        roof = {"kernel": "fstage_kernel (unpack+rotate+FFT+frac-delay)", "bound": "hbm",
+        roof = {"kernel": fkern + " (unpack+rotate+FFT+frac-delay)", "bound": "hbm",
                 "achieved": f_bytes / (f_launch_ms / 1e3) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "traffic": traffic("fstage_kernel"), "algorithmic_bytes_per_launch": f_bytes,
                 "launch_ms": f_launch_ms, "launches_per_step": nlaunch, "ffts_per_launch": ffts_per_launch,
