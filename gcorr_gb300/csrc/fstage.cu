@@ -130,16 +130,16 @@ cudaError_t launch_counts(const Job &job, int autos, int32_t *counts, uint8_t *v
 }
 
 // ----------------------------------------------------------------- twiddles
-// float2 slots that follow the F-point table when F = 8192: 256 float4 + 4096 float2.
+// float2 entries that follow the F-point table when F = 8192.
 constexpr int kPairTw1 = 16 * 16, kPairTw2 = 16 * 256;
 
 // tw[m] = exp(-2 pi i m / F), m < F, rounded once from double.  For F = 8192 the same
 // allocation continues with the pass twiddles W_M^e (M = F/2) of the packed-pair kernel,
 // laid out so that a warp reads consecutive entries:
-//   pass 1, [r][k]  (256 float4 broadcast pairs {c, c, s, s}): e = 16 r k, k < 16
-//   pass 2, [r][iv] (4096 float2 {c, s}, half the L1 footprint): e = r iv, iv < 256
+//   pass 1, [r][k]  (256 entries):  e = 16 r k, k < 16
+//   pass 2, [r][iv] (4096 entries): e = r iv,   iv < 256
 cudaError_t make_twiddles(int F, float2 **out) {
-  const size_t extra = F == 8192 ? 2 * (size_t)kPairTw1 + kPairTw2 : 0;
+  const size_t extra = F == 8192 ? (size_t)kPairTw1 + kPairTw2 : 0;
   std::vector<float2> h((size_t)F + extra);
   for (int m = 0; m < F; m++) {
     const double ang = -2.0 * 3.14159265358979323846 * (double)m / (double)F;
@@ -148,14 +148,9 @@ cudaError_t make_twiddles(int F, float2 **out) {
   if (extra) {
     auto wm = [&](int e) { return h[(size_t)((2 * (long long)e) % F)]; };  // W_M^e = W_F^(2e)
     for (int r = 0; r < 16; r++)
-      for (int k = 0; k < 16; k++) {
-        const float2 w = wm(16 * r * k);
-        const size_t slot = (size_t)F + 2 * ((size_t)r * 16 + k);
-        h[slot] = make_float2(w.x, w.x);
-        h[slot + 1] = make_float2(w.y, w.y);
-      }
+      for (int k = 0; k < 16; k++) h[(size_t)F + (size_t)r * 16 + k] = wm(16 * r * k);
     for (int r = 0; r < 16; r++)
-      for (int iv = 0; iv < 256; iv++) h[(size_t)F + 2 * kPairTw1 + (size_t)r * 256 + iv] = wm(r * iv);
+      for (int iv = 0; iv < 256; iv++) h[(size_t)F + kPairTw1 + (size_t)r * 256 + iv] = wm(r * iv);
   }
   cudaError_t e = cudaMalloc((void **)out, sizeof(float2) * h.size());
   if (e != cudaSuccess) return e;
@@ -281,7 +276,7 @@ template <> __device__ __forceinline__ __nv_fp8x2_e4m3 to_out<__nv_fp8x2_e4m3>(f
 struct FParams {
   Job job;
   const float2 *tw;    // W_F^m, m < F
-  const float4 *twq;   // F = 8192: pass-1 twiddles of the packed-pair kernel (make_twiddles), else null
+  const float2 *twp1;  // F = 8192: pass-1 twiddles of the packed-pair kernel (make_twiddles), else null
   const float2 *twp2;  // F = 8192: pass-2 twiddles of the packed-pair kernel, else null
   int t0, T;
   void *chan;
@@ -592,9 +587,14 @@ __device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) {
       : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
   return r;
 }
-// both lanes times w, given as the broadcast pairs WR = (w.re, w.re), WI = (w.im, w.im)
-__device__ __forceinline__ void pcmul(P2 &u, float2 WR, float2 WI) {
-  const float2 re = csub(pmul(u.re, WR), pmul(u.im, WI));
+// sign flip on the integer pipe (the FMA pipe is the kernel's busiest)
+__device__ __forceinline__ float negi(float x) { return __int_as_float(__float_as_int(x) ^ (int)0x80000000); }
+// both lanes times w = (wr, wi): four packed FMA-pipe instructions, as many pipe cycles as
+// two scalar complex products
+__device__ __forceinline__ void pcmul(P2 &u, float wr, float wi) {
+  const float nwi = negi(wi);
+  const float2 WR = make_float2(wr, wr), WI = make_float2(wi, wi), NWI = make_float2(nwi, nwi);
+  const float2 re = pfma(u.re, WR, pmul(u.im, NWI));
   u.im = pfma(u.re, WI, pmul(u.im, WR));
   u.re = re;
 }
@@ -799,8 +799,8 @@ __global__ void __launch_bounds__(256, 2) fstage_pair_kernel(FParams prm) {
     const int k = iv & (R - 1);
 #pragma unroll
     for (int r = 1; r < R; r++) {  // W_M^(16 r k)
-      const float4 w = __ldg(&prm.twq[16 * r + k]);
-      pcmul(u[r], make_float2(w.x, w.y), make_float2(w.z, w.w));
+      const float2 w = __ldg(&prm.twp1[16 * r + k]);
+      pcmul(u[r], w.x, w.y);
     }
     dft16p<false>(u);
   }
@@ -825,7 +825,7 @@ __global__ void __launch_bounds__(256, 2) fstage_pair_kernel(FParams prm) {
 #pragma unroll
     for (int r = 1; r < R; r++) {  // W_M^(r iv)
       const float2 w = __ldg(&prm.twp2[NB * r + iv]);
-      pcmul(u[r], make_float2(w.x, w.x), make_float2(w.y, w.y));
+      pcmul(u[r], w.x, w.y);
     }
     dft16p<!CPLX>(u);
     constexpr int RKEEP = CPLX ? R : R / 2;  // real data keeps channels c < N/2
@@ -1335,8 +1335,8 @@ cudaError_t launch_fstage(const Job &job, const float2 *twiddles, int t0, int nt
   FParams prm;
   prm.job = job;
   prm.tw = twiddles;
-  prm.twq = job.F == 8192 ? reinterpret_cast<const float4 *>(twiddles + job.F) : nullptr;
-  prm.twp2 = job.F == 8192 ? twiddles + job.F + 2 * kPairTw1 : nullptr;
+  prm.twp1 = job.F == 8192 ? twiddles + job.F : nullptr;
+  prm.twp2 = job.F == 8192 ? twiddles + job.F + kPairTw1 : nullptr;
   prm.t0 = t0;
   prm.T = T;
   prm.chan = chan;
