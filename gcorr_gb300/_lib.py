@@ -23,7 +23,8 @@ _STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4:
 
 # every function include/gxc.h declares (the CPU tests check the export list against the header)
 EXPORTS = [
-    "gxc_config_init", "gxc_validate_config", "gxc_input_bytes_per_antenna", "gxc_num_baselines",
+    "gxc_config_init", "gxc_validate_config", "gxc_input_bytes_per_antenna", "gxc_input_bytes_for_ffts",
+    "gxc_num_baselines",
     "gxc_status_string", "gxc_create", "gxc_destroy", "gxc_set_input", "gxc_set_delays", "gxc_process",
     "gxc_sync", "gxc_accumulate", "gxc_get_visibilities", "gxc_device_visibilities", "gxc_get_baseline_counts",
     "gxc_get_valid_flags", "gxc_last_error", "gxc_last_launch_count", "gxc_fft_block", "gxc_enable_stage_timing",
@@ -83,6 +84,8 @@ def lib():
         l.gxc_validate_config.restype = C.c_int
         l.gxc_input_bytes_per_antenna.argtypes = [P(GxcConfig)]
         l.gxc_input_bytes_per_antenna.restype = C.c_size_t
+        l.gxc_input_bytes_for_ffts.argtypes = [P(GxcConfig), P(C.c_double), P(C.c_double), C.c_int, C.c_int]
+        l.gxc_input_bytes_for_ffts.restype = C.c_longlong
         l.gxc_num_baselines.argtypes = [P(GxcConfig)]
         l.gxc_num_baselines.restype = C.c_int
         l.gxc_status_string.argtypes = [C.c_int]

@@ -149,6 +149,47 @@ gxc_status gxc_validate_config(const gxc_config *c) {
 
 size_t gxc_input_bytes_per_antenna(const gxc_config *c) { return c ? input_bytes(c) : 0; }
 
+// geometry_kernel: off(i) = i F - nd(i), nd(i) = int_rz((mean(i) - fso)/Ts + 0.5), where mean(i) is the
+// mean of the delay polynomial at i, i + 1/2 and i + 1 (FFT units), so it lies between the
+// polynomial's extremes on [t0, t0+nt].  Two samples of margin cover the rounding and the +-1
+// fix-ups; windows past maxoffset are flagged and read nothing.  The staging reads whole 16-byte
+// blocks.
+long long gxc_input_bytes_for_ffts(const gxc_config *c, const double *poly, const double *fso, int t0, int nt) {
+  if (!c || !poly || !fso || c->nant < 1 || c->nchan < 1 || c->nfft < 1 || c->bw_hz <= 0.0 || t0 < 0 || nt < 1 ||
+      (long long)t0 + nt > c->nfft)
+    return 0;
+  const long long total = (long long)input_bytes(c);
+  const long long F = fft_len(c);
+  const double Ts = c->is_complex ? 1.0 / c->bw_hz : 1.0 / (2.0 * c->bw_hz);
+  const long long maxoffset = (long long)(c->nfft - 1) * F;
+  const double x0 = (double)t0, x1 = (double)t0 + (double)nt;
+  long long need = 0;
+  for (int a = 0; a < c->nant; a++) {
+    const double p0 = poly[3 * a], p1 = poly[3 * a + 1], p2 = poly[3 * a + 2];
+    auto d = [&](double x) { return p0 * x * x + p1 * x + p2; };
+    double dmin = fmin(d(x0), d(x1)), dmax = fmax(d(x0), d(x1));
+    if (p0 != 0.0) {
+      const double xv = -p1 / (2.0 * p0);
+      if (xv > x0 && xv < x1) {
+        dmin = fmin(dmin, d(xv));
+        dmax = fmax(dmax, d(xv));
+      }
+    }
+    const double ndf_lo = (dmin - fso[a]) / Ts, ndf_hi = (dmax - fso[a]) / Ts;
+    if (!(fabs(ndf_lo) < 1.0e9) || !(fabs(ndf_hi) < 1.0e9)) return total;  // not finite: the whole buffer
+    const long long nd_min = (long long)floor(ndf_lo) - 2, nd_max = (long long)ceil(ndf_hi) + 2;
+    if ((long long)t0 * F - nd_max > maxoffset) continue;  // every window past the end: flagged
+    long long off = (long long)(t0 + nt - 1) * F - nd_min;
+    if (off > maxoffset) off = maxoffset;
+    if (off < 0) continue;  // every window before the start: flagged
+    const long long end = off + F + 1;  // samples
+    long long bytes = c->is_complex ? 4 * end : (end + 1) / 2;
+    bytes = (bytes + 15) / 16 * 16 + 16;
+    if (bytes > need) need = bytes;
+  }
+  return need < total ? need : total;
+}
+
 int gxc_num_baselines(const gxc_config *c) {
   if (!c || c->nant < 1) return 0;
   return c->nant * (c->nant - 1) / 2 + (c->autos ? c->nant : 0);
@@ -457,7 +498,8 @@ gxc_status gxc_process(gxc_handle *h, void *stream) { return gxc::process_chaine
 // process() with its host->device input copies ordered behind copy_wait (when given) and
 // followed by a record of copy_done (when given); batches use it to chain the jobs' copies.
 extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEvent_t copy_wait,
-                                             cudaEvent_t copy_done) {
+                                             cudaEvent_t copy_done, int nchunk, const cudaEvent_t *chunk_ev,
+                                             const long long *chunk_end) {
   if (!h) return GXC_ERR_INVALID_ARGUMENT;
   if (!h->have_input) return fail(h, GXC_ERR_STATE, "process() before set_input()");
   if (!h->have_delays) return fail(h, GXC_ERR_STATE, "process() before set_delays()");
@@ -518,9 +560,20 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
     h->ev_stage.assign((size_t)3 * h->nblocks, nullptr);
     for (auto &e : h->ev_stage) GXC_CUDA(h, cudaEventCreate(&e), "timing event");
   }
+  int waited = -1;  // input chunks already waited for
   for (int b = 0; b < h->nblocks; b++) {
     const int t0 = b * h->T;
     const int nt = (c.nfft - t0) < h->T ? (c.nfft - t0) : h->T;
+    if (nchunk > 0) {
+      // the first input chunk that holds every window of this block
+      const long long need = gxc_input_bytes_for_ffts(&c, h->poly.data(), h->fso.data(), t0, nt);
+      int j = 0;
+      while (j < nchunk - 1 && chunk_end[j] < need) j++;
+      if (j > waited) {
+        GXC_CUDA(h, cudaStreamWaitEvent(s, chunk_ev[j], 0), "ordering the input chunks");
+        waited = j;
+      }
+    }
     if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b], s), "timing event");
     GXC_CUDA(h, launch_fstage(h->job, h->d_tw, t0, nt, h->T, h->d_chan, h->chan_type, h->out_scale, s),
              "F-stage kernel");

@@ -89,8 +89,12 @@ int xstage_tensor_fits(int nant, int nchan, int chan_type);
 cudaError_t xstage_tensor_take_error(int *flag);
 
 // gxc_api.cu: process() with its host->device input copies ordered behind copy_wait (when not
-// null) and followed by a record of copy_done (when not null).
-gxc_status process_chained(gxc_handle *h, void *stream, cudaEvent_t copy_wait, cudaEvent_t copy_done);
+// null) and followed by a record of copy_done (when not null).  nchunk > 0: the device input
+// arrives in chunks, bytes [0, chunk_end[j]) of every antenna once chunk_ev[j] has completed; each
+// F-stage launch waits only for the chunk that holds its windows (gxc_input_bytes_for_ffts).
+gxc_status process_chained(gxc_handle *h, void *stream, cudaEvent_t copy_wait, cudaEvent_t copy_done,
+                           int nchunk = 0, const cudaEvent_t *chunk_ev = nullptr,
+                           const long long *chunk_end = nullptr);
 
 // Output baseline index of antennas j <= k (crosses in fxkernel order, then autos).
 __host__ __device__ inline int baseline_index(int j, int k, int nant) {

@@ -8,10 +8,12 @@
 // (fxkernel/src/testfxkernel.cpp:81-108).  Here the input of sub-integration
 // k+1 is copied on a copy stream into the second of `nslots` device input
 // slots while sub-integration k is correlated on the compute stream, so the
-// host->device traffic hides behind the F and X stages.  Per slot, two events
-// order the work: `loaded` (copy done, compute may start) and `consumed`
-// (compute done, the slot may be overwritten and the visibilities were
-// copied out).
+// host->device traffic hides behind the F and X stages.  Per slot, events
+// order the work: `consumed` (compute done, the slot may be overwritten and the
+// visibilities were copied out) and one per input chunk: the copy runs in time
+// order in kChunks pieces of every antenna, and each F-stage launch waits only
+// for the piece that holds its FFT windows (gxc_input_bytes_for_ffts), so the
+// correlation of a sub-integration starts while its later samples still load.
 //
 // Polarisation conversion follows the voltage-domain form of the reference's
 // linear2circular kernels (examples/chris/bench/gpubench.cu:145-160): per
@@ -105,6 +107,10 @@ unsigned grid_for(size_t n, int th) {
   return (unsigned)(g < 4096 ? (g ? g : 1) : 4096);
 }
 
+// input chunks per sub-integration (each at least kMinChunkBytes per antenna)
+constexpr int kChunks = 8;
+constexpr size_t kMinChunkBytes = 1 << 20;
+
 }  // namespace
 
 struct gxc_pipeline {
@@ -117,6 +123,8 @@ struct gxc_pipeline {
   size_t nvis_floats = 0;
   std::vector<uint8_t *> slot_buf;
   std::vector<cudaEvent_t> loaded, consumed;
+  int nchunk = 1;
+  std::vector<cudaEvent_t> chunk_ev;  // [slot][nchunk]: input bytes [0, chunk_end[j]) loaded
   std::vector<int64_t> slot_seq;
   cudaStream_t copy = nullptr, compute = nullptr;
   int64_t next_seq = 0;
@@ -148,6 +156,7 @@ void destroy_pipeline(gxc_pipeline *p) {
   for (uint8_t *b : p->slot_buf) cudaFree(b);
   for (cudaEvent_t e : p->loaded) cudaEventDestroy(e);
   for (cudaEvent_t e : p->consumed) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->chunk_ev) cudaEventDestroy(e);
   if (p->copy) cudaStreamDestroy(p->copy);
   if (p->compute) cudaStreamDestroy(p->compute);
   if (p->isum) cudaFree(p->isum);
@@ -177,6 +186,7 @@ gxc_status gxc_pipeline_create(const gxc_config *cfg, int nslots, int integrate,
   p->ant_stride = (p->bytes_per_ant + 255) / 256 * 256;
   p->nbl = gxc_num_baselines(cfg);
   p->nvis_floats = (size_t)p->nbl * 4 * cfg->nchan * 2;
+  p->nchunk = p->bytes_per_ant >= (size_t)kChunks * kMinChunkBytes ? kChunks : 1;
   cudaError_t e = cudaStreamCreateWithFlags(&p->copy, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->compute, cudaStreamNonBlocking);
   for (int s = 0; e == cudaSuccess && s < nslots; s++) {
@@ -188,6 +198,11 @@ gxc_status gxc_pipeline_create(const gxc_config *cfg, int nslots, int integrate,
     if (e == cudaSuccess) p->loaded.push_back(a);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b, cudaEventDisableTiming);
     if (e == cudaSuccess) p->consumed.push_back(b);
+    for (int j = 0; e == cudaSuccess && j < p->nchunk; j++) {
+      cudaEvent_t c = nullptr;
+      e = cudaEventCreateWithFlags(&c, cudaEventDisableTiming);
+      if (e == cudaSuccess) p->chunk_ev.push_back(c);
+    }
     p->slot_seq.push_back(-1);
   }
   if (e == cudaSuccess && integrate && p->nvis_floats) {
@@ -231,19 +246,34 @@ gxc_status gxc_pipeline_submit(gxc_pipeline *p, const uint8_t *const *inputs, co
   const int64_t seq = p->next_seq;
   const int slot = (int)(seq % p->nslots);
   uint8_t *buf = p->slot_buf[slot];
-  // copy stream: wait until the slot's previous sub-integration was correlated, then load it
+  // copy stream: wait until the slot's previous sub-integration was correlated, then load it in
+  // time order, chunk by chunk across the antennas
   PCUDA(p, cudaStreamWaitEvent(p->copy, p->consumed[slot], 0), "ordering the copy");
-  for (int a = 0; a < p->cfg.nant; a++)
-    PCUDA(p, cudaMemcpyAsync(buf + (size_t)a * p->ant_stride, inputs[a], p->bytes_per_ant, cudaMemcpyDefault, p->copy),
-          "copying input to the device");
+  const int nch = p->nchunk;
+  cudaEvent_t *cev = p->chunk_ev.data() + (size_t)slot * nch;
+  std::vector<long long> chunk_end(nch);
+  long long c0 = 0;
+  for (int j = 0; j < nch; j++) {
+    long long c1 = (long long)p->bytes_per_ant;
+    if (j < nch - 1) {
+      c1 = ((long long)p->bytes_per_ant * (j + 1) / nch + 4095) / 4096 * 4096;
+      if (c1 > (long long)p->bytes_per_ant) c1 = (long long)p->bytes_per_ant;
+    }
+    for (int a = 0; c1 > c0 && a < p->cfg.nant; a++)
+      PCUDA(p, cudaMemcpyAsync(buf + (size_t)a * p->ant_stride + c0, inputs[a] + c0, (size_t)(c1 - c0), cudaMemcpyDefault,
+                               p->copy),
+            "copying input to the device");
+    PCUDA(p, cudaEventRecord(cev[j], p->copy), "recording a load event");
+    chunk_end[j] = c1;
+    if (c1 > c0) c0 = c1;
+  }
   PCUDA(p, cudaEventRecord(p->loaded[slot], p->copy), "recording the load event");
-  // compute stream: wait for the load, correlate, post-process, copy out
-  PCUDA(p, cudaStreamWaitEvent(p->compute, p->loaded[slot], 0), "ordering the compute");
+  // compute stream: correlate (each F-stage launch waits for its input chunk), post-process, copy out
   std::vector<const uint8_t *> ptrs(p->cfg.nant);
   for (int a = 0; a < p->cfg.nant; a++) ptrs[a] = buf + (size_t)a * p->ant_stride;
   gxc_status st = gxc_set_input(p->h, ptrs.data(), p->bytes_per_ant);
   if (st == GXC_OK) st = gxc_set_delays(p->h, poly, fso);
-  if (st == GXC_OK) st = gxc_process(p->h, p->compute);
+  if (st == GXC_OK) st = gxc::process_chained(p->h, p->compute, nullptr, nullptr, nch, cev, chunk_end.data());
   if (st != GXC_OK) return pfail(p, st, std::string("process: ") + gxc_last_error(p->h));
   float *d_vis = const_cast<float *>(gxc_device_visibilities(p->h));
   const int th = 256;

@@ -84,6 +84,13 @@ gxc_status gxc_validate_config(const gxc_config *cfg);
 size_t gxc_input_bytes_per_antenna(const gxc_config *cfg);
 /* Output baselines: nant*(nant-1)/2 crosses (+ nant autos when enabled). */
 int gxc_num_baselines(const gxc_config *cfg);
+/* Bytes from the start of every antenna's input buffer that the FFTs [t0, t0+nt) of one
+ * sub-integration read, for the delay model (poly [nant][3], fso [nant]) as passed to
+ * gxc_set_delays: an upper bound from the delay polynomial's extremes over those FFTs (the exact
+ * windows, fxkernel/src/fxkernel.cpp:288-309, are computed on the device).  A caller that loads
+ * the input in time order may start the F-stage of those FFTs once this prefix of every antenna
+ * is in place; the streaming pipeline does so.  Returns 0 for invalid arguments. */
+long long gxc_input_bytes_for_ffts(const gxc_config *cfg, const double *poly, const double *fso, int t0, int nt);
 const char *gxc_status_string(gxc_status s);
 
 /* FxKernel::FxKernel (fxkernel/src/fxkernel.cpp:30-180): allocates device state. */

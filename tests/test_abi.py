@@ -94,3 +94,62 @@ def test_visibility_text_roundtrip(tmp_path):
     f, back = load_visibilities(str(p), 3)
     assert np.allclose(back, v, atol=1e-5)
     assert np.allclose(f, (np.arange(16) + 0.5) / 16 * 64.0)
+
+
+def _end_bytes_at(offset, F, is_complex):
+    end = 4 * (offset + F) if is_complex else (offset + F + 1) // 2
+    return (end + 15) // 16 * 16
+
+
+def _window_end_bytes(ocfg, poly3, fso, fft, F, is_complex):
+    """Last byte (exclusive) of the 16-byte staged window of one FFT, from the oracle's geometry
+    (fxkernel.cpp:288-309); 0 when the FFT is flagged."""
+    g = O.geometry(ocfg, poly3, fso, fft)
+    return _end_bytes_at(g.offset, F, is_complex) if g.valid else 0
+
+
+@pytest.mark.parametrize("is_complex", [False, True])
+@pytest.mark.parametrize("case", ["synth", "fast", "vertex", "flagged"])
+def test_input_bytes_for_ffts_bounds_every_window(is_complex, case):
+    """gxc_input_bytes_for_ffts (the streaming pipeline's per-block input bound) covers every
+    window the FFTs of the block read, and exceeds the tightest bound by little more than the
+    delay change over the block."""
+    import numpy as np
+    nchan, nfft, T = (512, 96, 12)
+    nbit = 8 if is_complex else 2
+    w = synth.Workload(nant=4, nchan=nchan, nfft=nfft, nbit=nbit, is_complex=is_complex, bw_hz=32e6, seed=7,
+                       offset_us=40.0)
+    poly, fso = synth.delay_model(w)
+    poly = np.array(poly, dtype=np.float64)
+    F = nchan if is_complex else 2 * nchan
+    Ts = 1.0 / 32e6 if is_complex else 1.0 / 64e6
+    fft_s = F * Ts
+    if case == "fast":      # delays sweeping several FFTs over the sub-integration, both signs
+        poly[:, 1] = np.array([3.0, -3.0, 1.5, -0.7]) * fft_s / 8
+    elif case == "vertex":  # a delay minimum inside the sub-integration
+        poly[:, 0] = 4.0 * fft_s / nfft ** 2
+        poly[:, 1] = -2.0 * poly[:, 0] * (nfft * np.array([0.3, 0.5, 0.55, 0.8]))
+    elif case == "flagged":  # windows pushed off both ends of the buffer
+        poly[:, 2] = np.array([-1.5, 1.5, 0.0, 0.2]) * nfft * fft_s
+    cfg = G.make_config(nant=4, nchan=nchan, nfft=nfft, nbit=nbit, is_complex=is_complex, bw=32e6)
+    ocfg = O.make_config(4, nchan, nfft, nbit, is_complex, 8.4e9, 32e6)
+    fsoa = np.ascontiguousarray(fso, dtype=np.float64)
+    P = C.POINTER(C.c_double)
+    total = L.lib().gxc_input_bytes_per_antenna(C.byref(cfg))
+    for t0 in range(0, nfft, T):
+        nt = min(T, nfft - t0)
+        got = L.lib().gxc_input_bytes_for_ffts(C.byref(cfg), poly.ctypes.data_as(P), fsoa.ctypes.data_as(P), t0, nt)
+        need = max(_window_end_bytes(ocfg, poly[a], fso[a], t, F, is_complex)
+                   for a in range(4) for t in range(t0, t0 + nt))
+        assert need <= got <= total, (t0, need, got)
+        # looseness: the delay change across the block (in bytes) plus the rounding margins
+        nd = [[round((np.polyval(poly[a], t + 0.5) - fso[a]) / Ts) for t in range(t0, t0 + nt)] for a in range(4)]
+        spread = max(max(v) - min(v) for v in nd)
+        per_sample = 4 if is_complex else 0.5
+        # a bound clamped at the last valid window (maxoffset) may exceed windows flagged off the end
+        clamp = _end_bytes_at((nfft - 1) * F, F, is_complex) + 16
+        if need > 0 and got < clamp:
+            assert got - need <= (spread + 8) * per_sample + 48, (t0, need, got, spread)
+    assert L.lib().gxc_input_bytes_for_ffts(C.byref(cfg), poly.ctypes.data_as(P), fsoa.ctypes.data_as(P), 0, 0) == 0
+    assert L.lib().gxc_input_bytes_for_ffts(C.byref(cfg), poly.ctypes.data_as(P), fsoa.ctypes.data_as(P),
+                                            nfft - 1, 2) == 0
