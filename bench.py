@@ -362,6 +362,23 @@ def run_batch_bench(args):
 
 
 # ---------------------------------------------------------------- GPU side
+def h2d_probe(buf, dev):
+    """Bandwidth of this machine's pinned host->device copy path, GB/s: one antenna's input
+    buffer copied alone three times (CUDA events), so an e2e figure can be read against it."""
+    d = torch.empty(buf.numel(), dtype=buf.dtype, device=dev)
+    d.copy_(buf, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(3):
+        d.copy_(buf, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    gbs = 3 * buf.numel() * buf.element_size() / (e0.elapsed_time(e1) / 1e3) / 1e9
+    del d
+    return gbs
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -488,6 +505,7 @@ def main():
     if not args.no_e2e:
         from gcorr_gb300.pipeline import Pipeline
         host = [x.cpu().pin_memory() for x in inputs_dev]
+        h2d_gbs = h2d_probe(host[0], dev)
         pipe = Pipeline(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, slots=2, integrate=False,
                         precision=args.precision, rotator="exact", autos=True, x_engine=args.x_engine,
                         fft_block=args.fft_block, device=local)
@@ -508,6 +526,7 @@ def main():
         e2e = {"value": samples * world / (ems / 1e3) / 1e9, "unit": "input Gsamples/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ems,
                "api": "gxc_pipeline_submit (2 input slots, copy/compute overlap)",
+               "h2d_probe_gbs": h2d_gbs,
                "matches_device_run": bool(np.array_equal(vis_h, vis0))}
         pipe.close()
 
