@@ -86,6 +86,19 @@ def test_antenna_counts_vs_fp64(nant):
     assert O.rel_rms_per_product(vis, ref).max() < FP32_TOL
 
 
+def test_fxkernel_rotator_8192_point_vs_port():
+    """The fxkernel-compatible rotator (its stride/substride table split and step quirk) through
+    the 8192-point packed-pair F-stage (2-bit real, nchan 4096 = 64^2; complex 8192 is not square):
+    crosses within the FP32 tolerance of the FP32 port of fxkernel's process(), counts bit-exact."""
+    w = synth.Workload(nant=3, nchan=4096, nfft=10, bw_hz=64e6, rho=0.3, seed=55, offset_us=5.0)
+    d = synth.generate(w)
+    inputs = [x.numpy() for x in d["inputs"]]
+    ref, rc = O.port_process(O.config_from_workload(w, O.ROT_FXKERNEL, False), inputs, d["poly"], d["fso"])
+    vis, counts, _ = _run(_wd(w), inputs, d["poly"], d["fso"], rotator="fxkernel", autos=False)
+    assert np.array_equal(counts, rc)
+    assert O.rel_rms_per_product(vis, ref).max() < FP32_TOL
+
+
 def test_8bit_complex_physics_vs_fp64():
     w = synth.Workload(nant=3, nchan=512, nfft=24, nbit=8, is_complex=True, bw_hz=32e6, rho=0.3, seed=77)
     d = synth.generate(w)
