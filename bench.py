@@ -308,6 +308,7 @@ def run_batch_bench(args):
         import ctypes as C
         from gcorr_gb300 import _lib as L
         host = [[x.cpu().pin_memory() for x in d["inputs"]] for d in data]
+        h2d_gbs = h2d_probe(max((x for hx in host for x in hx), key=lambda t: t.numel()), dev)
         bh = Batch([dict(j, inputs=hx) for j, hx in zip(jobs16, host)])
         outs = [torch.empty((bh.shapes[i][0] * 4 * bh.shapes[i][1],), dtype=torch.complex64).pin_memory()
                 for i in range(len(ws))]
@@ -330,6 +331,7 @@ def run_batch_bench(args):
                "h2d_bytes_per_step": int(sum(x.numel() for hx in host for x in hx)),
                "d2h_bytes_per_step": int(sum(o.numel() * 8 for o in outs)), "ms_per_step": ems,
                "api": "gxc_batch_launch on pinned host inputs (copies inside the graph)",
+               "h2d_probe_gbs": h2d_gbs,
                "matches_device_run": bool(all(np.array_equal(outs[i].numpy().reshape(vis16[i].shape), vis16[i])
                                               for i in range(len(ws))))}
         bh.close()
