@@ -367,6 +367,7 @@ def run_batch_bench(args):
 def h2d_probe(buf, dev):
     """Bandwidth of this machine's pinned host->device copy path, GB/s: one antenna's input
     buffer copied alone three times (CUDA events), so an e2e figure can be read against it."""
+    import torch
     d = torch.empty(buf.numel(), dtype=buf.dtype, device=dev)
     d.copy_(buf, non_blocking=True)
     torch.cuda.synchronize(dev)
