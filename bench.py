@@ -532,6 +532,27 @@ def main():
                "h2d_probe_gbs": h2d_gbs,
                "matches_device_run": bool(np.array_equal(vis_h, vis0))}
         pipe.close()
+        if world == 1:
+            # the drop-in path: FxKernel-style process() of one sub-integration on pinned host
+            # buffers (input copies in time-ordered chunks on the handle's copy stream), then the
+            # visibilities read back; one sub-integration at a time, nothing overlaps across steps
+            from gcorr_gb300 import FxKernel
+            fxh = FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=args.precision,
+                           rotator="exact", autos=True, x_engine=args.x_engine, fft_block=args.fft_block, device=local)
+            fxh.setInputData(host)
+            fxh.setDelays(d["poly"], d["fso"])
+            for _ in range(max(1, args.warmup)):
+                fxh.process()
+                fxh.visibilities()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                fxh.process()
+                vfx = fxh.visibilities()
+            fms = (time.perf_counter() - t0) / args.steps * 1e3
+            e2e["fxkernel_process"] = {"value": samples / (fms / 1e3) / 1e9, "ms_per_step": fms,
+                                       "api": "gxc_set_input (pinned host) + gxc_process + gxc_get_visibilities",
+                                       "matches_device_run": bool(np.array_equal(vfx, vis0))}
+            fxh.close()
 
     # roofline of the dominant kernel, per launch: algorithmic bytes of one launch (units = FFTs
     # of all streams it processes) over that kernel's average launch duration in the timed step

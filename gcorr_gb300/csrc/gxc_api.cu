@@ -9,6 +9,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -32,6 +33,12 @@ struct gxc_handle {
   bool input_on_host = false;
   bool have_input = false, have_delays = false;
   uint8_t *d_inbuf = nullptr;          // staging for host inputs [nant][bytes_per_ant]
+  // host inputs are copied on copy_stream in time-ordered chunks (in_chunk_ev[j]: every antenna's
+  // bytes [0, in_chunk_end[j]) are on the device); each F-stage block waits for its chunk
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr;
+  std::vector<cudaEvent_t> in_chunk_ev;
+  std::vector<long long> in_chunk_end;
   const uint8_t **d_inptrs = nullptr;  // device array of per-antenna device pointers
   double *d_poly = nullptr, *d_fso = nullptr;
   // frame validity (gxc_set_frame_validity): user device pointers, uploaded per process()
@@ -60,6 +67,10 @@ struct gxc_handle {
 };
 
 namespace {
+
+// time-ordered input chunks of host-input handles (each at least kMinInChunkBytes per antenna)
+constexpr int kInChunks = 8;
+constexpr size_t kMinInChunkBytes = 1 << 20;
 
 gxc_status fail(gxc_handle *h, gxc_status s, const std::string &msg) {
   if (h) h->err = msg;
@@ -230,6 +241,9 @@ static void release(gxc_handle *h) {
   cudaFree(h->d_vcomp);
   cudaFree(h->d_vis);
   if (h->ev_done) cudaEventDestroy(h->ev_done);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  for (cudaEvent_t e : h->in_chunk_ev) cudaEventDestroy(e);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   for (cudaEvent_t e : h->ev_stage) cudaEventDestroy(e);
   if (h->ev_begin) cudaEventDestroy(h->ev_begin);
   if (h->ev_end) cudaEventDestroy(h->ev_end);
@@ -405,6 +419,16 @@ gxc_status gxc_set_input(gxc_handle *h, const uint8_t *const *per_ant, size_t by
   if (h->input_on_host && !h->d_inbuf) {
     cudaError_t e = cudaMalloc((void **)&h->d_inbuf, h->bytes_per_ant * (size_t)h->cfg.nant);
     if (e != cudaSuccess) return cuda_fail(h, e, "allocating the device input buffer");
+    const int nch = h->bytes_per_ant >= (size_t)kInChunks * kMinInChunkBytes ? kInChunks : 1;
+    e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    for (int j = 0; e == cudaSuccess && j < nch; j++) {
+      cudaEvent_t c = nullptr;
+      e = cudaEventCreateWithFlags(&c, cudaEventDisableTiming);
+      if (e == cudaSuccess) h->in_chunk_ev.push_back(c);
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "creating the input copy stream");
+    h->in_chunk_end.assign((size_t)nch, 0);
   }
   h->have_input = true;
   return GXC_OK;
@@ -535,14 +559,38 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
     launches++;
   }
   if (h->input_on_host) {
-    if (copy_wait) GXC_CUDA(h, cudaStreamWaitEvent(s, copy_wait, 0), "ordering the input copies");
-    for (int a = 0; a < nant; a++)
-      GXC_CUDA(h,
-               cudaMemcpyAsync(h->d_inbuf + (size_t)a * h->bytes_per_ant, h->user_ptrs[a], h->bytes_per_ant,
-                               cudaMemcpyHostToDevice, s),
-               "copying input to the device");
+    // host inputs: copied on the handle's copy stream (forked from s) in time-ordered chunks, so
+    // the F-stage blocks below start while later samples still load
+    GXC_CUDA(h, cudaEventRecord(h->ev_fork, s), "forking the input copies");
+    GXC_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->ev_fork, 0), "forking the input copies");
+    if (copy_wait) GXC_CUDA(h, cudaStreamWaitEvent(h->copy_stream, copy_wait, 0), "ordering the input copies");
+    // inside a capture (batch graphs) one chunk: many small memcpy nodes cost the graph more than
+    // the overlap gains
+    const int nch = capturing ? 1 : (int)h->in_chunk_ev.size();
+    const long long bpa = (long long)h->bytes_per_ant;
+    long long c0 = 0;
+    for (int j = 0; j < nch; j++) {
+      long long c1 = bpa;
+      if (j < nch - 1) c1 = std::min(bpa, (bpa * (j + 1) / nch + 4095) / 4096 * 4096);
+      for (int a = 0; c1 > c0 && a < nant; a++)
+        GXC_CUDA(h,
+                 cudaMemcpyAsync(h->d_inbuf + (size_t)a * h->bytes_per_ant + c0, h->user_ptrs[a] + c0,
+                                 (size_t)(c1 - c0), cudaMemcpyHostToDevice, h->copy_stream),
+                 "copying input to the device");
+      // copy_done before the last chunk's event, so that the join on that event (below) also
+      // covers it inside a stream capture
+      if (j == nch - 1 && copy_done)
+        GXC_CUDA(h, cudaEventRecordWithFlags(copy_done, h->copy_stream, rec_flags), "recording the input copies");
+      GXC_CUDA(h, cudaEventRecord(h->in_chunk_ev[j], h->copy_stream), "recording an input chunk");
+      h->in_chunk_end[j] = c1;
+      if (c1 > c0) c0 = c1;
+    }
+    nchunk = nch;
+    chunk_ev = h->in_chunk_ev.data();
+    chunk_end = h->in_chunk_end.data();
+  } else if (copy_done) {
+    GXC_CUDA(h, cudaEventRecordWithFlags(copy_done, s, rec_flags), "recording the input copies");
   }
-  if (copy_done) GXC_CUDA(h, cudaEventRecordWithFlags(copy_done, s, rec_flags), "recording the input copies");
   if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_begin, s), "timing event");
 
   GXC_CUDA(h, launch_geometry(h->job, s), "geometry kernel");
@@ -598,6 +646,8 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
     }
     if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b + 2], s), "timing event");
   }
+  // join the input copies (the last blocks may not need the last chunk)
+  if (nchunk > 0) GXC_CUDA(h, cudaStreamWaitEvent(s, chunk_ev[nchunk - 1], 0), "joining the input copies");
   if (nvis > 0) {
     const int th = 256;
     finalize_kernel<<<(unsigned)((nvis + th - 1) / th), th, 0, s>>>(h->d_vsum, h->d_vcomp, h->d_counts, c.nchan,
