@@ -355,8 +355,10 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   A((void **)&h->d_valid, (size_t)nant * cfg->nfft);
   A(&h->d_chan, per_fft * (size_t)T);
   const size_t nvis = (size_t)(h->nbl > 0 ? h->nbl : 1) * 4 * cfg->nchan;
-  A((void **)&h->d_vsum, sizeof(float2) * nvis);
-  A((void **)&h->d_vcomp, sizeof(float2) * nvis);
+  // two accumulator planes: the tensor X-stage may split a block's FFTs across two CTAs per
+  // channel group (launch_xstage_tensor); finalisation sums the planes
+  A((void **)&h->d_vsum, sizeof(float2) * nvis * 2);
+  A((void **)&h->d_vcomp, sizeof(float2) * nvis * 2);
   A((void **)&h->d_vis, sizeof(float2) * nvis);
   if (e == cudaSuccess) e = make_twiddles(h->F, &h->d_tw);
   if (e == cudaSuccess) e = make_tile_pairs(nant, &h->d_pairs);
@@ -475,6 +477,8 @@ gxc_status gxc_set_delays(gxc_handle *h, const double *poly, const double *fso) 
 }
 
 // finalisation: vis = (sum + comp) * scale / count (fxkernel.cpp:358-367)
+// Sums the two accumulator planes (i and i + n) with a compensated add; a plane no launch wrote
+// is zero and leaves the result bit-identical to the first plane's.
 __global__ void finalize_kernel(const float2 *__restrict__ vsum, const float2 *__restrict__ vcomp,
                                 const int32_t *__restrict__ counts, int nchan, size_t n, float scale,
                                 float2 *__restrict__ vis) {
@@ -482,8 +486,11 @@ __global__ void finalize_kernel(const float2 *__restrict__ vsum, const float2 *_
   if (i >= n) return;
   const int bl = (int)(i / ((size_t)4 * nchan));
   const int cnt = counts[bl];
-  const float2 s = vsum[i], c = vcomp[i];
-  float re = (s.x + c.x) * scale, im = (s.y + c.y) * scale;
+  const float2 s0 = vsum[i], c0 = vcomp[i], s1 = vsum[i + n], c1 = vcomp[i + n];
+  float sx = s0.x, ex = c0.x, sy = s0.y, ey = c0.y;
+  two_sum_add(sx, ex, s1.x);
+  two_sum_add(sy, ey, s1.y);
+  float re = (sx + (ex + c1.x)) * scale, im = (sy + (ey + c1.y)) * scale;
   if (cnt > 0) {
     re /= (float)cnt;
     im /= (float)cnt;
@@ -600,8 +607,8 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
     launches++;
   }
   const size_t nvis = (size_t)h->nbl * 4 * c.nchan;
-  GXC_CUDA(h, cudaMemsetAsync(h->d_vsum, 0, sizeof(float2) * nvis, s), "clearing accumulators");
-  GXC_CUDA(h, cudaMemsetAsync(h->d_vcomp, 0, sizeof(float2) * nvis, s), "clearing accumulators");
+  GXC_CUDA(h, cudaMemsetAsync(h->d_vsum, 0, sizeof(float2) * nvis * 2, s), "clearing accumulators");
+  GXC_CUDA(h, cudaMemsetAsync(h->d_vcomp, 0, sizeof(float2) * nvis * 2, s), "clearing accumulators");
 
   if (timing && h->ev_stage.size() != (size_t)3 * h->nblocks) {
     for (cudaEvent_t e : h->ev_stage) cudaEventDestroy(e);
@@ -634,7 +641,7 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
         // is <= 2^ceil(log2F/2) * 182 <= 46592 < 65504, the FP16 maximum, for every F <= 32768.
         GXC_CUDA(h,
                  launch_xstage_tensor(h->d_chan, h->chan_type, nant, c.nchan, h->T, nt, c.autos, h->d_vsum,
-                                      h->d_vcomp, s, h->log2F / 2),
+                                      h->d_vcomp, s, h->log2F / 2, 2, nvis),
                  "tensor-core X-stage kernel");
       } else {
         GXC_CUDA(h,

@@ -247,6 +247,11 @@ struct Params {
   // FP16 hi/lo split (FP32 data of known scale): values are multiplied by split_sc (a power of
   // two) before the split, and the Gram sums by split_unsc (its inverse squared) at the end
   float split_sc, split_unsc;
+  // split of the block's FFTs across CTAs (FP16 / FP8 kernel): CTA b covers channel group
+  // b mod (grid/kparts) and FFTs [kspan*part, kspan*(part+1)) of the block, part = b / (grid/kparts),
+  // accumulating into plane `part` of vsum/vcomp (planes `plane` elements apart)
+  int kparts, kspan;
+  size_t plane;
 };
 
 // FP16 and FP8 paths: one accumulation over the whole FFT block (its TMEM rounding
@@ -268,9 +273,15 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
   const uint32_t sbase = smem_u32(smem);
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
-  const int cb = blockIdx.x * p.CS;  // first channel of this CTA
+  const int ngrp = (int)gridDim.x / p.kparts;
+  const int kpart = (int)blockIdx.x / ngrp;
+  const int cb = ((int)blockIdx.x - kpart * ngrp) * p.CS;  // first channel of this CTA
   const int n = p.nstream;
-  const int nchunks = (p.nt + KC - 1) / KC;
+  const int kt0 = kpart * p.kspan;  // first FFT of this CTA's share of the block
+  const int ntl = p.nt - kt0 < p.kspan ? p.nt - kt0 : p.kspan;
+  const int nchunks = (ntl + KC - 1) / KC;
+  float2 *const vsum = p.vsum + (size_t)kpart * p.plane;
+  float2 *const vcomp = p.vcomp + (size_t)kpart * p.plane;
 
   // zero the padding rows (2n..R-1 of each channel block) of the ring once; producers never write them
   if (2 * n < p.R) {
@@ -326,7 +337,7 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
         const uint32_t bar = smem_u32(&raw_full[rs]);
         mbar_expect_tx(bar, (uint32_t)(p.rbox_bytes * p.rnbox));
         for (int j = 0; j < p.rnbox; j++)
-          tma_load_4d(raw_s + rs * RAW_BYTES + j * p.rbox_bytes, &tmap, x0, 0, rc * KCR, (cb >> 4) + j, bar);
+          tma_load_4d(raw_s + rs * RAW_BYTES + j * p.rbox_bytes, &tmap, x0, 0, kt0 + rc * KCR, (cb >> 4) + j, bar);
         issued = rc + 1;
       }
       // every copy issued lands before the CTA can exit (the last RSTAGES are the only
@@ -505,11 +516,11 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
             }
             const int bl = baseline_index(j, k, p.nant);
             const size_t o = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
-            float2 sm = p.vsum[o], e = p.vcomp[o];
+            float2 sm = vsum[o], e = vcomp[o];
             two_sum_add(sm.x, e.x, re);
             two_sum_add(sm.y, e.y, im);
-            p.vsum[o] = sm;
-            p.vcomp[o] = e;
+            vsum[o] = sm;
+            vcomp[o] = e;
           }
         }
       }
@@ -1377,7 +1388,8 @@ int xstage_tensor_fits(int nant, int nchan, int chan_type) {
 }
 
 cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,
-                                 float2 *vsum, float2 *vcomp, cudaStream_t s, int split_e) {
+                                 float2 *vsum, float2 *vcomp, cudaStream_t s, int split_e, int kparts_max,
+                                 size_t plane) {
   if (nt <= 0) return cudaSuccess;
   if (!xstage_tensor_supported(nant)) return cudaErrorInvalidValue;
   tc::Params p;
@@ -1396,6 +1408,9 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   if (p.CS <= 0 || nchan % p.CS) return cudaErrorInvalidValue;
   p.vsum = vsum;
   p.vcomp = vcomp;
+  p.kparts = 1;
+  p.kspan = nt;
+  p.plane = plane;
   // FP32 data: FP16 hi/lo split of values scaled by 2^-split_e when split_e >= 0, else TF32 split
   const bool h16 = chan_type == CHAN_F32 && split_e >= 0;
   p.split_sc = h16 ? ldexpf(1.0f, -split_e) : 1.0f;
@@ -1458,10 +1473,24 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
     }
     if (e != cudaSuccess) return e;
   } else {
+    // one CTA per SM (its shared memory): when the channel groups leave SMs idle (fewer groups
+    // than SMs), split the block's FFTs in two halves, each into its own accumulator plane (with
+    // nt >= 4 KC both halves hold more than KC FFTs, so no CTA accumulates nothing).  Measured:
+    // 6 antennas (64 groups) FP16 0.49 -> 0.30 ms; with 512 groups (3.4 waves) the split was
+    // slower (9.0 -> 10.3 ms), its halved CTAs paying their pipeline fill and drain twice.
+    const int ngrp = nchan / p.CS;
+    int dev = 0, nsm = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    if (kparts_max >= 2 && plane > 0 && nt >= 4 * KC && ngrp < nsm) {
+      p.kparts = 2;
+      p.kspan = (nt / 2 + KC - 1) / KC * KC;
+    }
     auto kern = chan_type == CHAN_F8 ? tc::xstage_tc_kernel<true> : tc::xstage_tc_kernel<false>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<nchan / p.CS, tc::NTHREADS_TC, smem, s>>>(p, tmap);
+    kern<<<ngrp * p.kparts, tc::NTHREADS_TC, smem, s>>>(p, tmap);
   }
   return cudaGetLastError();
 }
