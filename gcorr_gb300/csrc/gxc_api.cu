@@ -421,15 +421,26 @@ gxc_status gxc_set_input(gxc_handle *h, const uint8_t *const *per_ant, size_t by
   if (h->input_on_host && !h->d_inbuf) {
     cudaError_t e = cudaMalloc((void **)&h->d_inbuf, h->bytes_per_ant * (size_t)h->cfg.nant);
     if (e != cudaSuccess) return cuda_fail(h, e, "allocating the device input buffer");
+  }
+  if (h->input_on_host && h->in_chunk_ev.empty()) {
+    // the copy stream and chunk events (created once; a failure leaves the handle without host
+    // input until a later call succeeds)
     const int nch = h->bytes_per_ant >= (size_t)kInChunks * kMinInChunkBytes ? kInChunks : 1;
-    e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    cudaError_t e = cudaSuccess;
+    if (!h->copy_stream) e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !h->ev_fork) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    std::vector<cudaEvent_t> evs;
     for (int j = 0; e == cudaSuccess && j < nch; j++) {
       cudaEvent_t c = nullptr;
       e = cudaEventCreateWithFlags(&c, cudaEventDisableTiming);
-      if (e == cudaSuccess) h->in_chunk_ev.push_back(c);
+      if (e == cudaSuccess) evs.push_back(c);
     }
-    if (e != cudaSuccess) return cuda_fail(h, e, "creating the input copy stream");
+    if (e != cudaSuccess) {
+      for (cudaEvent_t c : evs) cudaEventDestroy(c);
+      h->have_input = false;
+      return cuda_fail(h, e, "creating the input copy stream");
+    }
+    h->in_chunk_ev = evs;
     h->in_chunk_end.assign((size_t)nch, 0);
   }
   h->have_input = true;
@@ -534,6 +545,7 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
   if (!h) return GXC_ERR_INVALID_ARGUMENT;
   if (!h->have_input) return fail(h, GXC_ERR_STATE, "process() before set_input()");
   if (!h->have_delays) return fail(h, GXC_ERR_STATE, "process() before set_delays()");
+  if (h->input_on_host && h->in_chunk_ev.empty()) return fail(h, GXC_ERR_STATE, "host input without a copy stream");
   cudaSetDevice(h->device);
   cudaStream_t s = (cudaStream_t)stream;
   const gxc_config &c = h->cfg;
