@@ -6,10 +6,14 @@ FP32 end to end, 136 baselines (autos included) x 4 products.
 Metric: input Gsamples/s = nant * 2 pols * nfft * F / seconds per sub-integration.
 
 value: device-resident inputs, one process() per step, CUDA events on the
-launching stream.  e2e: the same call through the C ABI with pinned HOST input
-buffers (host->device copy inside process()) plus the device->host read of the
-visibilities, every step.  Multi-GPU (torchrun): independent replicas, one
-sub-integration per rank per step, no collective on the data path.
+launching stream.  e2e: the same sub-integration through the C ABI's streaming
+pipeline (gxc_pipeline_submit) from pinned HOST input buffers, the host->device
+copy of every step's input and the device->host read of its visibilities inside
+the timed region (wall clock); e2e.fxkernel_process: the drop-in path, one
+gxc_process on pinned host buffers plus the read-back per step; e2e.h2d_probe_gbs:
+the machine's pinned copy bandwidth, measured beside it.  Multi-GPU (torchrun):
+independent replicas, one sub-integration per rank per step, no collective on
+the data path.
 
 --impl reference times the CPU implementation of the path (the FP32 port of
 fxkernel in oracle/, all host threads) on a bounded sample of the same workload.
