@@ -1,0 +1,86 @@
+"""CPU checks of the index arithmetic of the packed-pair F-stage (fstage_pair_kernel in
+gcorr_gb300/csrc/fstage.cu), restated in numpy with the kernel's own index expressions:
+
+* pass 0: thread iv takes samples n = iv + 256 r (r < 32) and forms the two lanes
+  A = x[n] + x[n + M] and B = (x[n] - x[n + M]) W_N^(iv) W_32^r of the M = N/2-point sub-FFTs;
+* three radix-16 Stockham passes over the padded pair buffer (one slot of padding per 16),
+  with the pass twiddles read from the [r][k] tables make_twiddles builds;
+* sub-FFT bin kk = iv + 256 r of lane A is channel 2 kk, of lane B channel 2 kk + 1; real data
+  keeps r < 8 (channels below N/2).
+
+The transform must equal numpy's FFT, and every buffer index must stay inside the buffer.
+"""
+import numpy as np
+
+N, M, NT, R, PAD = 8192, 4096, 256, 16, 16
+NB = M // R          # butterflies per pass, one per thread
+NB0 = N // 32        # pass-0 sample stride
+PADM = M + M // PAD  # pair slots in shared memory
+
+
+def _dft16(u):
+    return np.fft.fft(u, axis=1)  # [thread][r][lane] -> DFT over r
+
+
+def _pair_fft(x):
+    WN = np.exp(-2j * np.pi * np.arange(N) / N)
+    WM = np.exp(-2j * np.pi * np.arange(M) / M)
+    tab1 = np.array([[WM[(16 * r * k) % M] for k in range(16)] for r in range(16)])    # [r][k]
+    tab2 = np.array([[WM[(r * iv) % M] for iv in range(256)] for r in range(16)])     # [r][iv]
+    iv = np.arange(NT)[:, None]
+    r = np.arange(R)[None, :]
+    buf = np.full((PADM, 2), np.nan + 0j)
+    # pass 0
+    x0, x1 = x[iv + NB0 * r], x[iv + NB0 * (r + R)]
+    w = WN[iv] * np.exp(-2j * np.pi * r / 32)                       # W_N^iv W_32^r
+    u = np.stack([x0 + x1, (x0 - x1) * w], axis=2)
+    u = _dft16(u)
+    idx0 = iv * (R + 1) + r
+    assert idx0.max() < PADM
+    buf[idx0] = u
+    # pass 1: radix 16, span 16, in place
+    ld = (iv + iv // PAD) + r * (NB + NB // PAD)
+    assert ld.max() < PADM
+    u = buf[ld]
+    k = iv & (R - 1)
+    u = u * tab1[r, k][:, :, None]
+    u = _dft16(u)
+    j = (iv - k) * R + k
+    st = (j + j // PAD) + r * (R + R // PAD)
+    assert st.max() < PADM and len(np.unique(st)) == NT * R
+    buf[st] = u
+    # pass 2: radix 16, span 256
+    u = buf[ld]
+    u = u * tab2[r, iv][:, :, None]
+    u = _dft16(u)
+    X = np.empty(N, complex)
+    kk = iv + r * NB
+    X[2 * kk] = u[:, :, 0]
+    X[2 * kk + 1] = u[:, :, 1]
+    return X
+
+
+def test_pair_plan_8192_matches_numpy_fft():
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    X = _pair_fft(x)
+    ref = np.fft.fft(x)
+    assert np.abs(X - ref).max() / np.abs(ref).max() < 1e-12
+
+
+def test_pair_plan_real_band_is_the_first_eight_outputs():
+    # channels below N/2 (a real band) come from r < 8 of the last pass, both lanes
+    kk = np.arange(NT)[:, None] + np.arange(8)[None, :] * NB
+    ch = np.concatenate([2 * kk.ravel(), 2 * kk.ravel() + 1])
+    assert np.array_equal(np.sort(ch), np.arange(N // 2))
+
+
+def test_pair_plan_twiddle_exponents_stay_in_the_tables():
+    # make_twiddles stores W_M^(16 r k) for k < 16 and W_M^(r iv) for iv < 256, r < 16
+    assert 16 * 15 * 15 < M and 15 * 255 < M
+    # pass-0 twiddle W_N^(iv + 256 r) = W_N^iv W_32^r for every sample pair of every thread
+    iv = np.arange(NT)[:, None]
+    r = np.arange(R)[None, :]
+    lhs = np.exp(-2j * np.pi * (iv + NB0 * r) / N)
+    rhs = np.exp(-2j * np.pi * iv / N) * np.exp(-2j * np.pi * r / 32)
+    assert np.abs(lhs - rhs).max() < 1e-12
