@@ -101,7 +101,9 @@ gxc_status gxc_destroy(gxc_handle *h);
 /* FxKernel::setInputData (fxkernel/src/fxkernel.cpp:242-245): per_ant[a] points at
  * bytes_per_ant bytes for antenna a, host (pageable or pinned) or device memory.
  * Device buffers are borrowed, must be 16-byte aligned and must outlive process(); host buffers are
- * copied to the device inside every process() call (host->device on the stream). */
+ * copied to the device inside every process() call, on the handle's own copy stream (forked from and
+ * joined back to the caller's stream) in time-ordered chunks that the F-stage starts on as they land;
+ * pinned host memory gives the fastest copies. */
 gxc_status gxc_set_input(gxc_handle *h, const uint8_t *const *per_ant, size_t bytes_per_ant);
 /* FxKernel::setDelays (fxkernel/src/fxkernel.cpp:247-251): poly [nant][3], fso [nant]
  * (host memory).  Values are copied at this call. */
