@@ -16,6 +16,8 @@ GXC_ERR_STATE = 5
 GXC_ERR_TIMEOUT = 6
 GXC_END_OF_DATA = 7
 GXC_PRECISION_FP32, GXC_PRECISION_FP16, GXC_PRECISION_FP8 = 0, 1, 2
+# size of gxc_xcorr_noalloc's fixed device scratch array (include/gxc.h)
+GXC_XCORR_NOALLOC_SCRATCH_BYTES = 16 << 20
 GXC_ROTATOR_EXACT, GXC_ROTATOR_FXKERNEL = 0, 1
 GXC_XENGINE_AUTO, GXC_XENGINE_CUDA_CORE, GXC_XENGINE_TENSOR = 0, 1, 2
 _STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "out of memory",
@@ -35,7 +37,7 @@ EXPORTS = [
     "gxc_conf_read", "gxc_conf_config", "gxc_conf_int", "gxc_conf_double", "gxc_conf_antenna_name",
     "gxc_conf_antenna_file", "gxc_conf_delays", "gxc_conf_free", "gxc_reader_open", "gxc_reader_read",
     "gxc_reader_close", "gxc_save_visibilities", "gxc_host_alloc", "gxc_host_free", "gxc_set_frame_validity",
-    "gxc_vdif_parse_header", "gxc_vdif_depacketize",
+    "gxc_vdif_parse_header", "gxc_vdif_depacketize", "gxc_probe_unpack",
 ]
 
 
@@ -116,6 +118,8 @@ def lib():
         l.gxc_last_error.restype = C.c_char_p
         l.gxc_last_launch_count.argtypes = [V]
         l.gxc_last_launch_count.restype = C.c_int
+        l.gxc_probe_unpack.argtypes = [V, V]
+        l.gxc_probe_unpack.restype = C.c_int
         l.gxc_fft_block.argtypes = [V]
         l.gxc_fft_block.restype = C.c_int
         l.gxc_enable_stage_timing.argtypes = [V, C.c_int]

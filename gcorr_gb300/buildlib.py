@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgxcorr.so")
-SOURCES = ["gxc_api.cu", "fstage.cu", "xstage_fp32.cu", "xstage_tc.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "batch_api.cu",
+SOURCES = ["gxc_api.cu", "fstage.cu", "fstage_probe.cu", "xstage_fp32.cu", "xstage_tc.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "batch_api.cu",
            "pipeline_api.cu", "conf_io.cpp", "vdif.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # command-line drivers with the reference harness's interface, linked against the library
@@ -45,7 +45,7 @@ def _needs(obj: str, deps) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "gxc.h"))
     jobs = []
     objs = []

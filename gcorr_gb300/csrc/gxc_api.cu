@@ -682,6 +682,34 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
   return GXC_OK;
 }
 
+gxc_status gxc_probe_unpack(gxc_handle *h, float *decoded) {
+  if (!h) return GXC_ERR_INVALID_ARGUMENT;
+  if (!decoded) return fail(h, GXC_ERR_INVALID_ARGUMENT, "null output");
+  if (h->have_input && h->input_on_host)
+    return fail(h, GXC_ERR_UNSUPPORTED, "the decode probe takes device inputs");
+  gxc_status st = gxc_process(h, nullptr);  // uploads pointers and delays, computes the geometry
+  if (st == GXC_OK) st = gxc_sync(h);
+  if (st != GXC_OK) return st;
+  const gxc_config &c = h->cfg;
+  const size_t n = (size_t)c.nant * 2 * c.nfft * h->F;
+  float2 *probe = nullptr;
+  void *chan = nullptr;
+  cudaError_t e = cudaMalloc((void **)&probe, n * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&chan, (size_t)h->T * c.nchan * 2 * c.nant * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemset(probe, 0xFF, n * sizeof(float2));  // NaN
+  for (int b = 0; e == cudaSuccess && b < h->nblocks; b++) {
+    const int t0 = b * h->T;
+    const int nt = (c.nfft - t0) < h->T ? (c.nfft - t0) : h->T;
+    e = launch_fstage_probe(h->job, h->d_tw, t0, nt, h->T, chan, h->chan_type, h->out_scale, probe, nullptr);
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(decoded, probe, n * sizeof(float2), cudaMemcpyDefault);
+  cudaFree(probe);
+  cudaFree(chan);
+  if (e != cudaSuccess) return cuda_fail(h, e, "decode probe");
+  return GXC_OK;
+}
+
 gxc_status gxc_sync(gxc_handle *h) {
   if (!h) return GXC_ERR_INVALID_ARGUMENT;
   if (!h->processed) return GXC_OK;

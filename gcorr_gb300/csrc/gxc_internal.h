@@ -65,6 +65,11 @@ cudaError_t make_twiddles(int F, float2 **out);
 cudaError_t launch_fstage(const Job &job, const float2 *twiddles, int t0, int nt, int T, void *chan, int chan_type,
                           float out_scale, cudaStream_t s);
 int fstage_supported(int F);
+// fstage_probe.cu: the F-stage of FFTs [t0, t0+nt) with every decoded input sample also written to
+// probe [nant][2][nfft][F] (complex float) before the fringe rotation.  chan must hold T FFTs of
+// FP32 channelised data.
+cudaError_t launch_fstage_probe(const Job &job, const float2 *twiddles, int t0, int nt, int T, void *chan,
+                                int chan_type, float out_scale, float2 *probe, cudaStream_t s);
 
 // xstage_fp32.cu: accumulates visibilities of FFTs [0, nt) of the block into
 // the compensated (sum, comp) accumulators in the output layout.

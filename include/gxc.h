@@ -139,6 +139,16 @@ gxc_status gxc_get_valid_flags(gxc_handle *h, uint8_t *flags);
 /* Text message of the last failing call on this handle ("" if none). */
 const char *gxc_last_error(const gxc_handle *h);
 
+/* Test entry for the unpack step: runs process() (device inputs only), then runs
+ * the F-stage kernels again with a probe that writes every decoded input sample,
+ * as the kernel holds it before the fringe rotation, to `decoded` (host or device):
+ * complex float [nant][2 pols][nfft][F].  The kernels are the production
+ * templates built with the probe write (the decode is the same code); samples of
+ * flagged FFTs stay NaN.  It replaces no reference member: it lets tests compare
+ * the GPU decode with the reference's unpack (fxkernel/src/fxkernel.cpp:15-28,
+ * :443-487) bit for bit.  Synchronous; allocates its scratch with cudaMalloc. */
+gxc_status gxc_probe_unpack(gxc_handle *h, float *decoded);
+
 /* Number of kernel launches the last process() enqueued (for accounting). */
 int gxc_last_launch_count(const gxc_handle *h);
 /* Effective FFT block (FFTs per F/X pass) chosen for this handle. */
@@ -298,14 +308,20 @@ gxc_status gxc_xcorr(const float *ants, int nant, int nfft, int nchan, int fftwi
  * callback or real-time ingest thread that must not block on the allocator,
  * which can synchronise the device; a process whose GPU memory budget belongs
  * to a framework that owns every allocation).  Same arguments and results as
- * gxc_xcorr with the CUDA-core engine, but ants and accum must already be
- * device memory, and the scratch lives in one fixed array of
- * GXC_XCORR_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library
- * until the process exits.  Problems whose accumulators (nbl*4*nchan complex
- * float, twice) plus one FFT of channelised data do not fit are rejected with
- * GXC_ERR_INVALID_ARGUMENT.  The call only enqueues work on `stream`.  The
- * first call on a device looks up the array's device address (do it before
- * any stream capture); calls that overlap on the GPU share the array and race. */
+ * gxc_xcorr with the CUDA-core engine, with these differences:
+ *   - precision GXC_PRECISION_FP32 or _FP16 only (FP8: GXC_ERR_UNSUPPORTED);
+ *   - ants and accum must be device memory of the current device (host buffers,
+ *     which gxc_xcorr stages, return GXC_ERR_INVALID_ARGUMENT);
+ *   - it only enqueues work on `stream`: synchronise before reading accum.
+ * The scratch lives in one fixed array of GXC_XCORR_NOALLOC_SCRATCH_BYTES held
+ * by every GPU that loads the library until the process exits.  Problems whose
+ * accumulators (nbl*4*nchan complex float, twice) plus one FFT of channelised
+ * data do not fit are rejected with GXC_ERR_INVALID_ARGUMENT.  The first call on
+ * a device looks up the array's device address and may load the library's device
+ * code: make it at initialisation, before any stream capture and outside any
+ * thread that must not block.  Calls after a cudaDeviceReset are not supported.
+ * All calls share the array: calls that overlap on the GPU (other streams or
+ * host threads) race on it, so serialise them on one stream. */
 #define GXC_XCORR_NOALLOC_SCRATCH_BYTES (16u << 20)
 gxc_status gxc_xcorr_noalloc(const float *ants, int nant, int nfft, int nchan, int fftwidth, int precision,
                              int autos, float *accum, void *stream);

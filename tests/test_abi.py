@@ -33,6 +33,13 @@ def test_library_exports_every_declared_symbol():
         assert re.search(rf"\bT {n}\b", out), n
 
 
+def test_header_constants_match_bindings():
+    txt = open(os.path.join(ROOT, "include", "gxc.h")).read()
+    m = re.search(r"#define GXC_XCORR_NOALLOC_SCRATCH_BYTES \((\d+)u << (\d+)\)", txt)
+    assert m, "scratch size define"
+    assert int(m.group(1)) << int(m.group(2)) == L.GXC_XCORR_NOALLOC_SCRATCH_BYTES
+
+
 def _status(**kw):
     cfg = G.make_config(**kw)
     return L.lib().gxc_validate_config(C.byref(cfg))

@@ -50,6 +50,60 @@ def test_golden_fxkernel_mode_matches_reference(golden_cases, engine):
 
 
 @pytest.mark.parametrize("engine", ["tensor", "cuda_core"])
+def test_benchmark_shapes_match_reference(shape_cases, engine):
+    """fxkernel rotator, crosses only, at the benchmark shapes: the reference's own process()
+    output for 6 antennas x nchan 1024 (2048-point FFTs) and 16 antennas x nchan 4096
+    (8192-point FFTs, the packed-pair F-stage), with flagged edge FFTs."""
+    from conftest import reference_checks
+    assert len(shape_cases) == 2
+    for name, d in shape_cases.items():
+        vis, counts, flags = _run(d, d["inputs"], d["poly"], d["fso"], rotator="fxkernel", autos=False,
+                                  x_engine=engine)
+        r = reference_checks(vis, d)
+        assert r["per_product"] < FP32_TOL and r.get("sum", 0.0) < FP32_TOL and r.get("power", 0.0) < FP32_TOL, \
+            (name, r)
+        assert np.array_equal(counts, d["counts"]), name
+        assert np.array_equal(flags, d["geom"][..., 1].astype(np.uint8)), name
+
+
+@pytest.mark.parametrize("engine", ["tensor", "cuda_core"])
+def test_benchmark_shapes_exact_mode_vs_fp64(shape_cases, engine):
+    for name, d in shape_cases.items():
+        cfg = O.make_config(int(d["nant"]), int(d["nchan"]), int(d["nfft"]), 2, False, float(d["lo_hz"]),
+                            float(d["bw_hz"]), O.ROT_EXACT, True)
+        ref, rc = O.exact_process(cfg, list(d["inputs"]), d["poly"], d["fso"])
+        vis, counts, _ = _run(d, d["inputs"], d["poly"], d["fso"], rotator="exact", autos=True, x_engine=engine)
+        assert np.array_equal(counts, rc), name
+        err = O.rel_rms_per_product(vis, ref)
+        assert err.max() < FP32_TOL, (name, err.max())
+
+
+# FP8 (E4M3, 3 mantissa bits) is reported with its measured error; this bound only catches breakage.
+FP8_TOL = 0.12
+
+
+@pytest.mark.parametrize("nant,nchan,nfft,is_complex,precision", [
+    (32, 8192, 8, False, "fp16"), (32, 8192, 8, False, "fp8"),
+    (64, 32768, 4, True, "fp16"), (64, 32768, 4, True, "fp8"),
+    (32, 16384, 4, True, "fp16")])
+def test_reduced_precision_large_arrays_vs_fp64(nant, nchan, nfft, is_complex, precision):
+    """FP16 and FP8 channelised data on the tensor-core X-stage at 32 and 64 antennas with
+    16384- and 32768-point windows (the FP16-buffer F-stage), against the FP64 oracle."""
+    w = synth.Workload(nant=nant, nchan=nchan, nfft=nfft, nbit=8 if is_complex else 2, is_complex=is_complex,
+                       bw_hz=128e6, rho=0.05, seed=nant * 7 + nfft, offset_us=2.0)
+    d = synth.generate(w)
+    inputs = [x.numpy() for x in d["inputs"]]
+    ref, rc = O.exact_process(O.config_from_workload(w, O.ROT_EXACT, True), inputs, d["poly"], d["fso"])
+    vis, counts, _ = _run(_wd(w), inputs, d["poly"], d["fso"], precision=precision, x_engine="tensor")
+    assert np.array_equal(counts, rc)
+    err = O.rel_rms_per_product(vis, ref)
+    nx = nant * (nant - 1) // 2
+    tol = FP16_TOL if precision == "fp16" else FP8_TOL
+    assert err.max() < tol, (err.max(), float(np.median(err)))
+    assert err[nx:].max() < tol / 4, err[nx:].max()  # power spectra
+
+
+@pytest.mark.parametrize("engine", ["tensor", "cuda_core"])
 def test_golden_exact_mode_matches_fp64_oracle(golden_cases, engine):
     for name, d in golden_cases.items():
         vis, counts, _ = _run(d, d["inputs"], d["poly"], d["fso"], rotator="exact", autos=True, x_engine=engine)

@@ -83,6 +83,28 @@ def test_fp64_oracle_compat_matches_reference_fixture(golden_cases):
         assert O.rel_rms(vis, d["ref_vis"]) < 2e-6, name
 
 
+def test_port_and_fp64_oracle_match_benchmark_shaped_fixtures(shape_cases):
+    """The oracle pinned at the benchmark shapes: the reference's own process() output for 6
+    antennas x nchan 1024 (2048-point FFTs, flagged edge FFTs) and 16 antennas x nchan 4096
+    (8192-point FFTs), fxkernel rotator, crosses only."""
+    from conftest import reference_checks
+    assert set(shape_cases) == {"shape_c0_6ant_n1024", "shape_c1_16ant_n4096"}
+    for name, d in shape_cases.items():
+        cfg = _cfg(d, O.ROT_FXKERNEL, False)
+        vis, counts = O.port_process(cfg, list(d["inputs"]), d["poly"], d["fso"], nthreads=4)
+        assert np.array_equal(counts, d["counts"]), name
+        r = reference_checks(vis, d)
+        assert r["per_product"] < 1e-5 and r.get("sum", 0.0) < 1e-6 and r.get("power", 0.0) < 1e-5, (name, r)
+        ve, ce = O.exact_process(cfg, list(d["inputs"]), d["poly"], d["fso"])
+        assert np.array_equal(ce, d["counts"]), name
+        r = reference_checks(ve, d)
+        assert r["per_product"] < 1e-5 and r.get("sum", 0.0) < 1e-6 and r.get("power", 0.0) < 1e-5, (name, r)
+        for a in range(int(d["nant"])):
+            for i in range(int(d["nfft"])):
+                g = O.geometry(cfg, d["poly"][a], float(d["fso"][a]), i)
+                assert g.valid == d["geom"][a, i, 1] and (not g.valid or g.offset == d["geom"][a, i, 0]), (name, a, i)
+
+
 def test_exact_fixture_reproducible(golden_cases):
     for name, d in golden_cases.items():
         cfg = _cfg(d, O.ROT_EXACT, True)
