@@ -15,8 +15,10 @@ the machine's pinned copy bandwidth, measured beside it.  Multi-GPU (torchrun):
 independent replicas, one sub-integration per rank per step, no collective on
 the data path.
 
---impl reference times the CPU implementation of the path (the FP32 port of
-fxkernel in oracle/, all host threads) on a bounded sample of the same workload.
+--impl reference times the CPU implementation of the path on all host threads on
+a bounded sample of the same workload: the reference's own fxkernel.cpp (compiled
+unmodified by oracle/Makefile, one FxKernel per thread) for the jobs it can run,
+the FP32 port of it (oracle/fxoracle.c) for the others.
 """
 from __future__ import annotations
 
@@ -39,6 +41,11 @@ CONFIGS = {
            "in one graph launch", "config3_jobs"),
     "c4": ("64 antennas, 8-bit complex, 256 Ms/s per pol, 0.5 s, nchan 32768, rho 0.02", "config4"),
 }
+
+
+# the X engines every bench run compares (untimed side runs)
+XENGINES = (("fp32_cuda_core", "fp32", "cuda_core"), ("fp32_tensor_split", "fp32", "tensor"),
+            ("fp16_tensor", "fp16", "tensor"), ("fp8_tensor", "fp8", "tensor"))
 
 
 def dist_env():
@@ -166,44 +173,109 @@ def cpu_port_run(w, nfft_sample: int, nthreads: int, seed_inputs=None):
     return samples / dt, dt, seed_inputs
 
 
-def cpu_sample(w, budget_s: float = 12.0):
-    """Picks a bounded FFT sample taking about budget_s of CPU work on all threads."""
-    nthreads = os.cpu_count() or 1
-    n = 8 * nthreads
-    rate, dt, _ = cpu_port_run(w, n, nthreads)
-    per_fft = dt / n
-    n2 = int(max(n, min(w.nfft, budget_s / max(per_fft, 1e-6))))
+def cpu_model() -> str:
+    """The host CPU as the OS reports it (model name, or the Arm implementer/part codes)."""
+    try:
+        txt = open("/proc/cpuinfo").read()
+    except OSError:
+        return "unknown"
+    import re
+    m = re.search(r"^model name\s*:\s*(.+)$", txt, re.M)
+    if m:
+        return m.group(1).strip()
+    impl = re.search(r"^CPU implementer\s*:\s*(\S+)", txt, re.M)
+    part = re.search(r"^CPU part\s*:\s*(\S+)", txt, re.M)
+    arm = {("0x41", "0xd4f"): "Arm Neoverse-V2", ("0x41", "0xd40"): "Arm Neoverse-V1", ("0x41", "0xd0c"): "Arm Neoverse-N1"}
+    if impl and part:
+        key = (impl.group(1).lower(), part.group(1).lower())
+        return arm.get(key, f"Arm implementer {key[0]} part {key[1]}")
+    return "unknown"
+
+
+def ref_runnable(w) -> bool:
+    """The reference's own process() runs 2-bit real data with a square nchan only
+    (fxkernel/src/fxkernel.cpp:46-63, :489-496)."""
+    from oracle import oracle as O
+    return O.ref_bench_available() and not w.is_complex and w.nbit == 2 and int(round(w.nchan ** 0.5)) ** 2 == w.nchan
+
+
+def cpu_ref_run(w, nfft_sample: int, nthreads: int, seed_inputs=None):
+    """Times the reference's own process() (float-FFT shim build, one FxKernel per thread over
+    contiguous FFT slices) on nfft_sample FFTs of workload w."""
+    import dataclasses
+    from gcorr_gb300 import synth
+    from oracle import oracle as O
+    ws = dataclasses.replace(w, nfft=nfft_sample)
+    if seed_inputs is None:
+        d = synth.random_bytes(ws)
+        seed_inputs = ([x.numpy() for x in d["inputs"]], d["poly"], d["fso"])
+    inputs, poly, fso = seed_inputs
+    dt = O.ref_bench(ws.nant, ws.nchan, ws.lo_hz, ws.bw_hz, inputs, poly, fso, 0, ws.nfft, nthreads)
+    samples = ws.nant * 2 * ws.nfft * ws.fft_len
+    return samples / dt, dt, seed_inputs
+
+
+def _sized_run(run, w, budget_s: float, nthreads: int):
+    n = 4 * nthreads
+    _, dt, _ = run(w, n, nthreads)
+    n2 = int(max(n, min(w.nfft, budget_s / max(dt / n, 1e-6))))
     n2 -= n2 % nthreads if n2 > nthreads else 0
-    rate, dt, _ = cpu_port_run(w, n2, nthreads)
-    return {"value": rate / 1e9, "unit": "input Gsamples/s", "cores": nthreads, "kind": "port",
-            "sample": f"{n2} of {w.nfft} FFTs of the same workload (random 2-bit bytes, fxkernel-rotator FP32 port, "
+    rate, dt, _ = run(w, n2, nthreads)
+    return rate, dt, n2
+
+
+def cpu_sample(w, budget_s: float = 12.0):
+    """The CPU baseline on a bounded FFT sample of the workload (about budget_s of CPU work on all
+    host threads): the reference's own fxkernel.cpp where it can run the workload and its sources
+    were staged (kind "reference"), else the FP32 port of it (kind "port"); with the reference,
+    the port is timed beside it on the same sample size."""
+    nthreads = os.cpu_count() or 1
+    host = {"cores": nthreads, "nproc": nthreads, "cpu_model": cpu_model()}
+    if ref_runnable(w):
+        rate, dt, n2 = _sized_run(cpu_ref_run, w, budget_s, nthreads)
+        prate, pdt, _ = cpu_port_run(w, n2, nthreads)
+        return {"value": rate / 1e9, "unit": "input Gsamples/s", "kind": "reference", **host,
+                "sample": f"{n2} of {w.nfft} FFTs of the same workload (random 2-bit bytes): the reference's "
+                          f"fxkernel.cpp, unmodified, one FxKernel per thread over contiguous FFT slices, IPP "
+                          f"unavailable (float-FFT shim), {nthreads} threads, {dt:.1f} s",
+                "seconds": dt, "port": {"value": prate / 1e9, "seconds": pdt, "kind": "port"}}
+    rate, dt, n2 = _sized_run(cpu_port_run, w, budget_s, nthreads)
+    return {"value": rate / 1e9, "unit": "input Gsamples/s", "kind": "port", **host,
+            "sample": f"{n2} of {w.nfft} FFTs of the same workload (random bytes, FP32 port of fxkernel, "
                       f"{nthreads} threads), {dt:.1f} s", "seconds": dt}
 
 
 def port_plan(ws, budget_s: float, nthreads: int):
-    """Bounded sample of a list of jobs: the same fraction of every job's FFTs, sized so
-    one pass of the FP32 port over all of them takes about budget_s on nthreads threads."""
+    """Bounded sample of a list of jobs: the same fraction of every job's FFTs, sized so that one
+    pass over all of them takes about budget_s on nthreads threads.  Each job runs on the
+    reference's own code where it can (ref_runnable), else on the FP32 port."""
     cal = []
     for w in ws:
+        run = cpu_ref_run if ref_runnable(w) else cpu_port_run
         n0 = max(1, min(w.nfft, nthreads))
-        _, dt, seed = cpu_port_run(w, n0, nthreads)
-        cal.append((w, dt / n0, seed))
-    full = sum(per * w.nfft for w, per, _ in cal)
+        _, dt, _ = run(w, n0, nthreads)
+        cal.append((w, run, dt / n0))
+    full = sum(per * w.nfft for w, _, per in cal)
     frac = min(1.0, budget_s / max(full, 1e-9))
     plan = []
-    for w, per, _ in cal:
+    for w, run, per in cal:
         n = int(max(min(w.nfft, nthreads), min(w.nfft, round(frac * w.nfft))))
         n -= n % nthreads if n > nthreads else 0
-        _, _, seed = cpu_port_run(w, n, nthreads)
-        plan.append((w, n, seed))
+        _, _, seed = run(w, n, nthreads)
+        plan.append((w, n, seed, run))
     return plan
+
+
+def plan_kind(plan) -> str:
+    kinds = {"reference" if run is cpu_ref_run else "port" for _, _, _, run in plan}
+    return kinds.pop() if len(kinds) == 1 else "reference+port"
 
 
 def run_plan(plan, nthreads):
     t = 0.0
     samples = 0
-    for w, n, seed in plan:
-        _, dt, _ = cpu_port_run(w, n, nthreads, seed)
+    for w, n, seed, run in plan:
+        _, dt, _ = run(w, n, nthreads, seed)
         t += dt
         samples += w.nant * 2 * n * w.fft_len
     return samples, t
@@ -230,16 +302,20 @@ def run_reference_arm(args):
         tot += t_
         samples += s_
     val = samples / tot / 1e9
-    sample = "; ".join(f"{n} of {j.nfft} FFTs" for j, n, _ in plan)
+    kind = plan_kind(plan)
+    sample = "; ".join(f"{n} of {j.nfft} FFTs ({'reference' if run is cpu_ref_run else 'port'})"
+                       for j, n, _, run in plan)
     line = {"impl": "reference", "metric": "input Gsamples/s", "value": val, "unit": "input Gsamples/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": CONFIGS[args.config][0], "sample_ffts_per_step": [n for _, n, _ in plan],
+            "config": {"workload": CONFIGS[args.config][0], "sample_ffts_per_step": [n for _, n, _, _ in plan],
                        "nfft": [j.nfft for j in ws], "parallelism": "host threads"},
-            "cpu_baseline": {"value": val, "unit": "input Gsamples/s", "cores": nthreads, "kind": "port",
-                             "sample": f"{sample} per step, FP32 port of fxkernel (oracle/fxoracle.c), "
-                                       f"{nthreads} threads (IPP unavailable)"},
+            "cpu_baseline": {"value": val, "unit": "input Gsamples/s", "cores": nthreads, "nproc": nthreads,
+                             "cpu_model": cpu_model(), "kind": kind,
+                             "sample": f"{sample} per step; reference = fxkernel.cpp unmodified, one FxKernel per "
+                                       f"thread over contiguous FFT slices (float-FFT shim, IPP unavailable); "
+                                       f"port = FP32 restatement of it (oracle/fxoracle.c); {nthreads} threads"},
             "e2e": {"value": val, "unit": "input Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -345,9 +421,11 @@ def run_batch_bench(args):
         nthreads = os.cpu_count() or 1
         plan = port_plan(ws, 12.0, nthreads)
         cs, ct = run_plan(plan, nthreads)
-        cpu = {"value": cs / ct / 1e9, "unit": "input Gsamples/s", "cores": nthreads, "kind": "port",
-               "sample": "; ".join(f"{n} of {j.nfft} FFTs" for j, n, _ in plan)
-                         + f" (random bytes, FP32 port of fxkernel, {nthreads} threads), {ct:.1f} s"}
+        cpu = {"value": cs / ct / 1e9, "unit": "input Gsamples/s", "cores": nthreads, "nproc": nthreads,
+               "cpu_model": cpu_model(), "kind": plan_kind(plan),
+               "sample": "; ".join(f"{n} of {j.nfft} FFTs ({'reference' if run is cpu_ref_run else 'port'})"
+                                   for j, n, _, run in plan)
+                         + f" (random bytes, {nthreads} threads), {ct:.1f} s"}
     if rank == 0:
         pk = peaks()
         line = {
@@ -368,6 +446,74 @@ def run_batch_bench(args):
 
 
 # ---------------------------------------------------------------- GPU side
+def sample_errors(w, inputs_dev, poly, fso, args, device, engines=()):
+    """Per-product error of the benchmarked path on a sample of the benchmarked workload: FFTs
+    [s0, s0+S) from the middle of the sub-integration (the input windows sliced out of the same
+    device buffers, the delay polynomial re-expanded about s0), run through the library at the
+    bench's precision and engine, against the FP64 oracle (exact rotator, autos included) and,
+    with the fxkernel rotator (2-bit real, square nchan), against the reference's own process()
+    (oracle/_ref, unmodified fxkernel.cpp) or, where its sources were not staged, the FP32 port.
+    Errors are relative RMS over channels per (baseline, product): max and median over products.
+    engines: further (name, precision, x_engine) runs compared with the same FP64 oracle output."""
+    import dataclasses
+    import numpy as np
+    from gcorr_gb300 import FxKernel
+    from oracle import oracle as O
+    nprod = 4 * w.nant * (w.nant + 1) // 2
+    S = int(max(2, min(32, 1.5e9 // (nprod * w.nchan), w.nfft)))
+    s0 = (w.nfft - S) // 2
+    bpf = w.bytes_per_antenna // (w.nfft + 1)
+    sl = [x[s0 * bpf:(s0 + S + 1) * bpf] for x in inputs_dev]
+    host = [x.cpu().numpy() for x in sl]
+    p = np.asarray(poly, dtype=np.float64)
+    q = p.copy()
+    q[:, 1] = p[:, 1] + 2.0 * p[:, 0] * s0
+    q[:, 2] = p[:, 2] + p[:, 1] * s0 + p[:, 0] * s0 * s0
+    ws = dataclasses.replace(w, nfft=S)
+
+    def gpu(rotator, autos, precision=args.precision, x_engine=args.x_engine):
+        fx = FxKernel(w.nant, w.nchan, S, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=precision,
+                      rotator=rotator, autos=autos, x_engine=x_engine, device=device)
+        fx.setInputData(sl)
+        fx.setDelays(q, fso)
+        fx.process()
+        v, c = fx.visibilities(), fx.baseline_counts()
+        fx.close()
+        return v, c
+
+    def stats(e, nx):
+        return {"max": float(e.max()), "median": float(np.median(e)), "crosses_max": float(e[:nx].max()),
+                "crosses_median": float(np.median(e[:nx])) if nx else None,
+                "autos_max": float(e[nx:].max()) if e.shape[0] > nx else None}
+
+    nx = w.nant * (w.nant - 1) // 2
+    t0 = time.perf_counter()
+    vis, cnt = gpu("exact", True)
+    ref, rc = O.exact_process(O.config_from_workload(ws, O.ROT_EXACT, True), host, q, fso)
+    out = {"ffts": S, "first_fft": s0, "precision": args.precision,
+           "vs_fp64": dict(stats(O.rel_rms_per_product(vis, ref), nx), counts_equal=bool(np.array_equal(cnt, rc)))}
+    if not w.is_complex and w.nbit == 2 and int(round(w.nchan ** 0.5)) ** 2 == w.nchan and nx > 0:
+        vis2, _ = gpu("fxkernel", False)
+        if O.ref_available():
+            ref2, kind = O.ref_process(w.nant, w.nchan, S, w.lo_hz, w.bw_hz, host, q, fso), "reference"
+        else:
+            ref2, _ = O.port_process(O.config_from_workload(ws, O.ROT_FXKERNEL, False), host, q, fso)
+            kind = "port"
+        out["vs_fxkernel"] = dict(stats(O.rel_rms_per_product(vis2, ref2), nx), kind=kind)
+    if engines:
+        out["engines"] = {}
+        for name, prec, eng in engines:
+            try:
+                v, c = gpu("exact", True, prec, eng)
+            except Exception as ex:  # engine not available for this shape
+                out["engines"][name] = {"error": str(ex)[:120]}
+                continue
+            out["engines"][name] = dict(stats(O.rel_rms_per_product(v, ref), nx),
+                                        counts_equal=bool(np.array_equal(c, rc)))
+    out["seconds"] = time.perf_counter() - t0
+    return out
+
+
 def h2d_probe(buf, dev):
     """Bandwidth of this machine's pinned host->device copy path, GB/s: one antenna's input
     buffer copied alone three times (CUDA events), so an e2e figure can be read against it."""
@@ -401,8 +547,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-xcompare", action="store_true")
+    ap.add_argument("--no-errors", action="store_true", help="skip the per-product error sample")
     ap.add_argument("--ref-step-s", type=float, default=6.0)
-    ap.add_argument("--out-dir", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--out-dir", default=os.path.join(ROOT, "bench_out"), help="clock samples are written here")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -476,8 +623,7 @@ def main():
     # X-stage comparison (untimed): the same sub-integration through each X engine
     xcmp = {}
     if not args.no_xcompare:
-        for name, prec, eng in (("fp32_cuda_core", "fp32", "cuda_core"), ("fp32_tensor_split", "fp32", "tensor"),
-                                ("fp16_tensor", "fp16", "tensor"), ("fp8_tensor", "fp8", "tensor")):
+        for name, prec, eng in XENGINES:
             try:
                 fy = G.FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=prec,
                                 rotator="exact", autos=True, x_engine=eng, fft_block=args.fft_block, device=local)
@@ -608,6 +754,10 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_sample(w)
+    errs = None
+    if rank == 0 and not args.no_errors:
+        errs = sample_errors(w, inputs_dev, d["poly"], d["fso"], args, local,
+                             engines=() if args.no_xcompare else XENGINES)
 
     if rank == 0:
         line = {
@@ -624,6 +774,7 @@ def main():
                              f"{chan_bytes / 1e9:.1f} GB channelised per step)"},
             "stage_ms": {"f": f_ms, "x": x_ms, "total": tot_ms},
             "x_engines": xcmp,
+            "errors": errs,
             "x_tflops": xflops / (x_ms / 1e3) / 1e12,
             "gpu_launches": launches_per_step * args.steps,
             "roofline": roof,

@@ -14,7 +14,10 @@
 // this library, for the life of the process.  Host code cannot use its name
 // as a device address, so the first call on each device looks the address up
 // with cudaGetSymbolAddress (with that device current) and caches it; make
-// that first call before any stream capture.  All calls share the array and
+// that first call at initialisation, before any stream capture and outside any
+// thread that must not block (it may load this module's device code, which
+// allocates the array).  A cudaDeviceReset invalidates the cached address:
+// calls after one are not supported.  All calls share the array and
 // leave their data in it: accumulators are cleared at the start of every call,
 // and calls that overlap on the GPU (different streams, or concurrent host
 // threads) race on it.
@@ -92,13 +95,17 @@ __global__ void divide_noalloc_kernel(const float2 *__restrict__ vsum, const flo
   out[i] = make_float2((s.x + c.x) / nfft, (s.y + c.y) / nfft);
 }
 
+// Device memory of the current device (whose scratch array the call uses), or managed memory.
 bool on_device(const void *p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  int cur = -1;
+  if (cudaGetDevice(&cur) != cudaSuccess) return false;
+  return a.type == cudaMemoryTypeDevice && a.device == cur;
 }
 
 gxc_status fail(gxc_status st, const std::string &msg) {
@@ -117,7 +124,8 @@ extern "C" gxc_status gxc_xcorr_noalloc(const float *ants, int nant, int nfft, i
   if (precision != GXC_PRECISION_FP32 && precision != GXC_PRECISION_FP16)
     return fail(GXC_ERR_UNSUPPORTED, "precision must be FP32 or FP16");
   if (!on_device(ants) || !on_device(accum))
-    return fail(GXC_ERR_INVALID_ARGUMENT, "ants and accum must be device memory (nothing is staged)");
+    return fail(GXC_ERR_INVALID_ARGUMENT,
+                "ants and accum must be device memory of the current device (nothing is staged)");
 
   const int nstream = 2 * nant;
   const int nat = (nant + 1) / 2;

@@ -9,9 +9,13 @@
  * configurations it rejects (fxkernel/src/fxkernel.cpp:46-63) and unpack()
  * only handles 2-bit data (:489-496), so those cases are refused here first.
  */
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
+#include <vector>
 #include "fxkernel.h"
 
 extern "C" {
@@ -85,6 +89,64 @@ int fxref_save(int nant, int nchan, int nfft, int nbit, double lo, double bw, in
   delete[] offsets;
   delete[] idata;
   return 0;
+}
+
+/* CPU baseline: the reference's thread replication (fxkernel/src/bench_fxkernel.cpp:93-139), one
+ * FxKernel per thread, each constructed and given its delays before the clock starts.  Thread t
+ * processes FFTs [fft0 + t*nfft/nthreads, fft0 + (t+1)*nfft/nthreads) of the sub-integration whose
+ * buffers are `inputs` (each holding at least (fft0+nfft+1) FFT windows): its input pointers start
+ * at the slice's first window and its delay polynomial is re-expanded about the slice's first FFT
+ * (t -> t + start).  Returns the wall-clock seconds from the common start to the last thread's end
+ * of process(), or a negative value when the reference cannot run the case. */
+double fxref_bench(int nant, int nchan, int nbit, double lo, double bw, int iscomplex, const uint8_t *const *inputs,
+                   const double *poly, const double *fso, int fft0, int nfft, int nthreads) {
+  if (nbit != 2 || iscomplex) return -2.0;
+  int s = (int)std::sqrt((double)nchan);
+  if (s * s != nchan) return -3.0;
+  if (nant < 2 || nfft < 1 || nthreads < 1 || fft0 < 0) return -4.0;
+  if (nthreads > nfft) nthreads = nfft;
+  const long long F = 2LL * nchan;
+  const long long bytes_per_fft = F * 2 * nbit / 8;  // 2 pols of F real samples
+  struct Slice {
+    FxKernel *fx = nullptr;
+    std::vector<u8 *> idata;
+    std::vector<double *> dptr;
+    std::vector<double> d, off;
+  };
+  std::vector<Slice> sl((size_t)nthreads);
+  for (int t = 0; t < nthreads; t++) {
+    const int b = fft0 + (int)((long long)nfft * t / nthreads), e = fft0 + (int)((long long)nfft * (t + 1) / nthreads);
+    Slice &x = sl[(size_t)t];
+    x.fx = new FxKernel(nant, nchan, e - b, nbit, lo, bw, false);
+    x.idata.resize((size_t)nant);
+    x.d.resize((size_t)nant * 3);
+    x.dptr.resize((size_t)nant);
+    x.off.assign(fso, fso + nant);
+    const double sb = (double)b;
+    for (int a = 0; a < nant; a++) {
+      x.idata[(size_t)a] = const_cast<u8 *>(inputs[a]) + (long long)b * bytes_per_fft;
+      const double p0 = poly[3 * a], p1 = poly[3 * a + 1], p2 = poly[3 * a + 2];
+      x.d[3 * (size_t)a] = p0;
+      x.d[3 * (size_t)a + 1] = p1 + 2.0 * p0 * sb;
+      x.d[3 * (size_t)a + 2] = p2 + p1 * sb + p0 * sb * sb;
+      x.dptr[(size_t)a] = &x.d[3 * (size_t)a];
+    }
+    x.fx->setDelays(x.dptr.data(), x.off.data());
+    x.fx->setInputData(x.idata.data());
+  }
+  std::atomic<int> go(0);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; t++)
+    th.emplace_back([&, t] {
+      while (!go.load(std::memory_order_acquire)) std::this_thread::yield();
+      sl[(size_t)t].fx->process();
+    });
+  const auto t0 = std::chrono::steady_clock::now();
+  go.store(1, std::memory_order_release);
+  for (auto &x : th) x.join();
+  const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  for (auto &x : sl) delete x.fx;
+  return dt;
 }
 
 }  // extern "C"

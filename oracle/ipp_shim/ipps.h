@@ -155,6 +155,8 @@ typedef struct IppsFFTSpec_C_32fc {
   int flag;
   double *tw_re; /* e^{-2 pi i k/n}, k < n/2 */
   double *tw_im;
+  float *twf;    /* the same twiddles rounded to float, interleaved re, im */
+  int *bitrev;   /* bit-reversed index of every i < n */
 } IppsFFTSpec_C_32fc;
 
 static inline IppStatus ippsFFTGetSize_C_32fc(int order, int flag, IppHintAlgorithm hint,
@@ -162,7 +164,7 @@ static inline IppStatus ippsFFTGetSize_C_32fc(int order, int flag, IppHintAlgori
   (void)flag; (void)hint;
   if (order < 0 || order > 27) return ippStsFftOrderErr;
   int n = 1 << order;
-  *pSpecSize = (int)(sizeof(IppsFFTSpec_C_32fc) + 64 + (size_t)n * sizeof(double));
+  *pSpecSize = (int)(sizeof(IppsFFTSpec_C_32fc) + 3 * 64 + (size_t)n * (sizeof(double) + sizeof(float) + sizeof(int)));
   *pSpecBufferSize = 0;
   /* work buffer: two complex-double arrays of n */
   *pBufferSize = (int)((size_t)n * 4 * sizeof(double) + 64);
@@ -181,15 +183,60 @@ static inline IppStatus ippsFFTInit_C_32fc(IppsFFTSpec_C_32fc **ppSpec, int orde
   base = (base + 63) & ~(uintptr_t)63;
   s->tw_re = (double *)base;
   s->tw_im = s->tw_re + (s->n / 2 > 0 ? s->n / 2 : 1);
+  const int nh = s->n / 2 > 0 ? s->n / 2 : 1;
+  s->twf = (float *)(((uintptr_t)(s->tw_im + nh) + 63) & ~(uintptr_t)63);
+  s->bitrev = (int *)(((uintptr_t)(s->twf + 2 * nh) + 63) & ~(uintptr_t)63);
   for (int k = 0; k < s->n / 2; k++) {
     double ang = -2.0 * 3.14159265358979323846264338327950288 * (double)k / (double)s->n;
     s->tw_re[k] = cos(ang);
     s->tw_im[k] = sin(ang);
+    s->twf[2 * k] = (float)s->tw_re[k];
+    s->twf[2 * k + 1] = (float)s->tw_im[k];
+  }
+  for (int i = 0; i < s->n; i++) {
+    unsigned r = 0, v = (unsigned)i;
+    for (int b = 0; b < order; b++) { r = (r << 1) | (v & 1u); v >>= 1; }
+    s->bitrev[i] = (int)r;
   }
   *ppSpec = s;
   return ippStsNoErr;
 }
 
+#ifdef GXC_SHIM_FFT_F32
+/* Iterative radix-2 decimation-in-time FFT in single precision (float twiddles, float
+ * butterflies): the CPU-baseline build, closer to IPP's own float arithmetic and speed than the
+ * double-precision default below. */
+static inline IppStatus ippsFFTFwd_CToC_32fc(const Ipp32fc *src, Ipp32fc *dst, const IppsFFTSpec_C_32fc *s,
+                                             Ipp8u *buf) {
+  const int n = s->n;
+  float *x = (float *)(((uintptr_t)buf + 63) & ~(uintptr_t)63); /* interleaved re, im */
+  for (int i = 0; i < n; i++) {
+    const int r = s->bitrev[i];
+    x[2 * r] = src[i].re;
+    x[2 * r + 1] = src[i].im;
+  }
+  for (int len = 2; len <= n; len <<= 1) {
+    const int half = len >> 1, step = n / len;
+    for (int i = 0; i < n; i += len) {
+      float *a = x + 2 * i, *b = x + 2 * (i + half);
+      for (int j = 0; j < half; j++) {
+        const float wr = s->twf[2 * j * step], wi = s->twf[2 * j * step + 1];
+        const float xr = b[2 * j], xi = b[2 * j + 1];
+        const float vr = xr * wr - xi * wi, vi = xr * wi + xi * wr;
+        const float ur = a[2 * j], ui = a[2 * j + 1];
+        a[2 * j] = ur + vr; a[2 * j + 1] = ui + vi;
+        b[2 * j] = ur - vr; b[2 * j + 1] = ui - vi;
+      }
+    }
+  }
+  const float scale = s->flag == IPP_FFT_DIV_FWD_BY_N ? 1.0f / (float)n : 1.0f;
+  for (int i = 0; i < n; i++) {
+    dst[i].re = x[2 * i] * scale;
+    dst[i].im = x[2 * i + 1] * scale;
+  }
+  return ippStsNoErr;
+}
+#else
 /* Iterative radix-2 decimation-in-time FFT in double precision. */
 static inline IppStatus ippsFFTFwd_CToC_32fc(const Ipp32fc *src, Ipp32fc *dst, const IppsFFTSpec_C_32fc *s,
                                              Ipp8u *buf) {
@@ -225,6 +272,7 @@ static inline IppStatus ippsFFTFwd_CToC_32fc(const Ipp32fc *src, Ipp32fc *dst, c
   }
   return ippStsNoErr;
 }
+#endif
 
 #ifdef __cplusplus
 }

@@ -3,7 +3,9 @@
 * ``liboracle.so`` — the C restatement in fxoracle.c: the FP32 port of
   FxKernel::process() (fxkernel/src/fxkernel.cpp:253-368) and the FP64 oracle.
 * ``_ref/libfxref.so`` — the reference's own fxkernel.cpp compiled unmodified
-  against the IPP-compatible shim (only where the reference sources exist).
+  against the IPP-compatible shim (only where oracle/Makefile found the
+  reference sources); ``_ref/libfxref_f32.so`` the same with the shim's
+  float-internal FFT, timed as the CPU baseline.
 
 Only tests/, the smoke entry point and bench.py's CPU-baseline / reference arm
 use this module; the GPU engine never does.
@@ -19,6 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfxref.so")
+REF_F32_SO = os.path.join(HERE, "_ref", "libfxref_f32.so")
 
 ROT_EXACT = 0
 ROT_FXKERNEL = 1
@@ -46,6 +49,7 @@ def build(force: bool = False) -> None:
 
 _lib = None
 _ref = None
+_ref32 = None
 
 
 def lib():
@@ -89,6 +93,30 @@ def ref():
                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p]
         _ref = R
     return _ref
+
+
+def ref_bench_available() -> bool:
+    return os.path.exists(REF_F32_SO)
+
+
+def ref_bench(nant, nchan, lo_hz, bw_hz, inputs, poly, fso, fft0: int, nfft: int, nthreads: int) -> float:
+    """Seconds the reference's own process() (float-FFT shim build) takes for FFTs [fft0, fft0+nfft)
+    of a 2-bit real sub-integration, one FxKernel per thread over contiguous FFT slices, as
+    fxkernel/src/bench_fxkernel.cpp:93-139 replicates it."""
+    global _ref32
+    if _ref32 is None:
+        R = C.CDLL(REF_F32_SO)
+        R.fxref_bench.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]
+        R.fxref_bench.restype = C.c_double
+        _ref32 = R
+    arrs, ptrs = _inputs_array(inputs)
+    poly, fso = _f64(poly), _f64(fso)
+    dt = _ref32.fxref_bench(int(nant), int(nchan), 2, float(lo_hz), float(bw_hz), 0, ptrs, poly.ctypes.data,
+                            fso.ctypes.data, int(fft0), int(nfft), int(nthreads))
+    if dt < 0:
+        raise ValueError(f"reference cannot run this case ({dt})")
+    return dt
 
 
 def make_config(nant, nchan, nfft, nbit=2, is_complex=False, lo_hz=8.4e9, bw_hz=64e6,
