@@ -240,6 +240,16 @@ def ref_process(nant, nchan, nfft, lo_hz, bw_hz, inputs, poly, fso):
     return vis
 
 
+def ref_save(nant, nchan, nfft, lo_hz, bw_hz, inputs, poly, fso, path: str) -> None:
+    """The reference's process() then saveVisibilities(path) (fxkernel/src/fxkernel.cpp:370-412)."""
+    arrs, ptrs = _inputs_array(inputs)
+    poly, fso = _f64(poly), _f64(fso)
+    rc = ref().fxref_save(int(nant), int(nchan), int(nfft), 2, float(lo_hz), float(bw_hz), 0, ptrs,
+                          poly.ctypes.data, fso.ctypes.data, path.encode())
+    if rc:
+        raise ValueError(f"reference cannot run this case ({rc})")
+
+
 def rel_rms(a, b) -> float:
     """||a-b|| / ||b|| over all elements."""
     a = np.asarray(a).astype(np.complex128)
