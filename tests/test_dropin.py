@@ -81,9 +81,8 @@ def test_reference_testfxkernel_on_engine_matches_reference_vis_out(tmp_path):
     f1, v1 = visio.load_visibilities(str(tmp_path / "vis.out"), nbl)
     f2, v2 = visio.load_visibilities(ref_path, nbl)
     assert np.array_equal(f1, f2)
-    # 5 printed decimals: the engine's FP32 result and the reference's differ by < 1e-5 relative
-    assert np.allclose(v1, v2, rtol=2e-5, atol=2e-5)
-    assert O.rel_rms_per_product(v1, v2).max() < 1e-4
+    # the FP32 tolerance of the parity tests, per (baseline, product), on the printed values
+    assert O.rel_rms_per_product(v1, v2).max() < 1e-5
 
 
 @needs_staged
