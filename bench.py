@@ -473,7 +473,7 @@ def sample_errors(w, inputs_dev, poly, fso, args, device, engines=()):
 
     def gpu(rotator, autos, precision=args.precision, x_engine=args.x_engine):
         fx = FxKernel(w.nant, w.nchan, S, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=precision,
-                      rotator=rotator, autos=autos, x_engine=x_engine, device=device)
+                      rotator=rotator, autos=autos, x_engine=x_engine, device=device, fft_engine=args.fft_engine)
         fx.setInputData(sl)
         fx.setDelays(q, fso)
         fx.process()
@@ -541,6 +541,8 @@ def main():
     ap.add_argument("--config", default="c1", choices=sorted(CONFIGS))
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "fp8"])
     ap.add_argument("--x-engine", default="auto", choices=["auto", "cuda_core", "tensor"])
+    ap.add_argument("--fft-engine", default="auto", choices=["auto", "cuda_core", "tensor"],
+                    help="F-stage FFT: tensor cores (8192-point FP16/FP8) or CUDA cores")
     ap.add_argument("--fft-block", type=int, default=0)
     ap.add_argument("--nfft", type=int, default=0, help="override the FFT count (small profiling captures)")
     ap.add_argument("--nchan", type=int, default=0, help="override the channel count (small profiling captures)")
@@ -580,7 +582,8 @@ def main():
     stream = torch.cuda.Stream(device=dev)
 
     fx = G.FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=args.precision,
-                    rotator="exact", autos=True, x_engine=args.x_engine, fft_block=args.fft_block, device=local)
+                    rotator="exact", autos=True, x_engine=args.x_engine, fft_block=args.fft_block, device=local,
+                    fft_engine=args.fft_engine)
     fx.setInputData(inputs_dev)
     fx.setDelays(d["poly"], d["fso"])
     sptr = stream.cuda_stream
@@ -626,7 +629,8 @@ def main():
         for name, prec, eng in XENGINES:
             try:
                 fy = G.FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=prec,
-                                rotator="exact", autos=True, x_engine=eng, fft_block=args.fft_block, device=local)
+                                rotator="exact", autos=True, x_engine=eng, fft_block=args.fft_block, device=local,
+                                fft_engine=args.fft_engine)
             except Exception as ex:  # engine not available for this shape
                 xcmp[name] = {"error": str(ex)[:120]}
                 continue
@@ -661,7 +665,7 @@ def main():
         h2d_gbs = h2d_probe(host[0], dev)
         pipe = Pipeline(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, slots=2, integrate=False,
                         precision=args.precision, rotator="exact", autos=True, x_engine=args.x_engine,
-                        fft_block=args.fft_block, device=local)
+                        fft_block=args.fft_block, device=local, fft_engine=args.fft_engine)
         outs = [torch.empty((pipe.nbl, 4, w.nchan), dtype=torch.complex64).pin_memory() for _ in range(2)]
         for i in range(args.warmup):
             pipe.submit(host, d["poly"], d["fso"], out=outs[i % 2])
@@ -688,7 +692,8 @@ def main():
             # visibilities read back; one sub-integration at a time, nothing overlaps across steps
             from gcorr_gb300 import FxKernel
             fxh = FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=args.precision,
-                           rotator="exact", autos=True, x_engine=args.x_engine, fft_block=args.fft_block, device=local)
+                           rotator="exact", autos=True, x_engine=args.x_engine, fft_block=args.fft_block, device=local,
+                           fft_engine=args.fft_engine)
             fxh.setInputData(host)
             fxh.setDelays(d["poly"], d["fso"])
             for _ in range(max(1, args.warmup)):
@@ -728,7 +733,10 @@ def main():
         return None if not t else t["per_fft"] * ffts_per_launch + t.get("per_launch_const", 0)
 
     # the F-stage kernel this FFT length and precision runs
-    if w.fft_len == 8192:
+    tc_f = (w.fft_len == 8192 and not w.is_complex and args.precision != "fp32" and args.fft_engine == "tensor")
+    if tc_f:
+        fkern = "fstage_tc_kernel"
+    elif w.fft_len == 8192:
         fkern = "fstage_pair_kernel"
     elif w.fft_len >= 16384 and args.precision != "fp32":
         fkern = "fstage_h_kernel"
@@ -743,6 +751,12 @@ def main():
                 "launch_ms": f_launch_ms, "launches_per_step": nlaunch, "ffts_per_launch": ffts_per_launch,
                 "fft_tflops": fftflops / (f_ms / 1e3) / 1e12, "fp32_peak_tflops_nominal": fp32_peak}
         roof["fp32_pipe_frac_nominal"] = roof["fft_tflops"] / fp32_peak
+        if tc_f:
+            # issued MMA work of the four-step DFT products: per window (both pols) 2 x 2*128*128*128
+            # (step 1) + 2*128*128*256 (step 2) flops
+            mma_flops = w.nant * w.nfft * (2 * 2 * 128 ** 3 + 2 * 128 * 128 * 256)
+            roof["mma_tflops"] = mma_flops / (f_ms / 1e3) / 1e12
+            roof["mma_frac_of_bf16_peak"] = roof["mma_tflops"] / pk["bf16_tflops"]
     else:
         roof = {"kernel": "xstage", "bound": "hbm", "achieved": x_bytes / (x_launch_ms / 1e3) / 1e9,
                 "peak": pk["hbm_gbs"], "unit": "GB/s", "traffic": traffic("xstage"),
@@ -768,7 +782,8 @@ def main():
             "data": "synthetic",
             "config": {"workload": CONFIGS[args.config][0], "nant": w.nant, "nchan": w.nchan, "nfft": w.nfft,
                        "fft_len": w.fft_len, "nbit": w.nbit, "precision": args.precision,
-                       "x_engine": args.x_engine, "fft_block": fx.fft_block, "autos": True,
+                       "x_engine": args.x_engine, "fft_engine": args.fft_engine, "fft_block": fx.fft_block,
+                       "autos": True,
                        "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 ({in_bytes / 1e9:.1f} GB packed, "
                              f"{chan_bytes / 1e9:.1f} GB channelised per step)"},

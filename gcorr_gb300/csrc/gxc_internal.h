@@ -71,6 +71,13 @@ int fstage_supported(int F);
 cudaError_t launch_fstage_probe(const Job &job, const float2 *twiddles, int t0, int nt, int T, void *chan,
                                 int chan_type, float out_scale, float2 *probe, cudaStream_t s);
 
+// fstage_tc.cu: the tensor-core F-stage (8192-point windows, 2-bit real, FP16 / FP8 output).
+int fstage_tc_supported(const Job &job, int chan_type);
+cudaError_t make_fstage_tc_tables(void **out);  // its constant operands (cudaMalloc'd; caller frees)
+cudaError_t launch_fstage_tc(const Job &job, const void *tables, int t0, int nt, int T, void *chan, int chan_type,
+                             float out_scale, cudaStream_t s);
+cudaError_t fstage_tc_take_error(int *flag);
+
 // xstage_fp32.cu: accumulates visibilities of FFTs [0, nt) of the block into
 // the compensated (sum, comp) accumulators in the output layout.
 cudaError_t launch_xstage_cuda_core(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,

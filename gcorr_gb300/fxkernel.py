@@ -20,10 +20,12 @@ from . import _lib as L
 PRECISION = {"fp32": L.GXC_PRECISION_FP32, "fp16": L.GXC_PRECISION_FP16, "fp8": L.GXC_PRECISION_FP8}
 ROTATOR = {"exact": L.GXC_ROTATOR_EXACT, "fxkernel": L.GXC_ROTATOR_FXKERNEL}
 XENGINE = {"auto": L.GXC_XENGINE_AUTO, "cuda_core": L.GXC_XENGINE_CUDA_CORE, "tensor": L.GXC_XENGINE_TENSOR}
+FFTENGINE = {"auto": L.GXC_FFT_AUTO, "cuda_core": L.GXC_FFT_CUDA_CORE, "tensor": L.GXC_FFT_TENSOR}
 
 
 def make_config(nant, nchan, nfft, nbit=2, lo=8.4e9, bw=64e6, is_complex=False, precision="fp32",
-                rotator="exact", autos=True, x_engine="auto", fft_block=0, device=-1) -> L.GxcConfig:
+                rotator="exact", autos=True, x_engine="auto", fft_block=0, device=-1,
+                fft_engine="auto") -> L.GxcConfig:
     cfg = L.GxcConfig()
     L.lib().gxc_config_init(C.byref(cfg))
     cfg.nant, cfg.nchan, cfg.nfft, cfg.nbit = int(nant), int(nchan), int(nfft), int(nbit)
@@ -35,6 +37,7 @@ def make_config(nant, nchan, nfft, nbit=2, lo=8.4e9, bw=64e6, is_complex=False, 
     cfg.x_engine = XENGINE[x_engine] if isinstance(x_engine, str) else int(x_engine)
     cfg.fft_block = int(fft_block)
     cfg.device = int(device)
+    cfg.fft_engine = FFTENGINE[fft_engine] if isinstance(fft_engine, str) else int(fft_engine)
     return cfg
 
 
@@ -54,9 +57,9 @@ class FxKernel:
 
     def __init__(self, nant: int, nchan: int, nfft: int, nbit: int, lo: float, bw: float, is_complex: bool = False,
                  *, precision: str = "fp32", rotator: str = "exact", autos: bool = True, x_engine: str = "auto",
-                 fft_block: int = 0, device: int = -1):
+                 fft_block: int = 0, device: int = -1, fft_engine: str = "auto"):
         self.cfg = make_config(nant, nchan, nfft, nbit, lo, bw, is_complex, precision, rotator, autos, x_engine,
-                               fft_block, device)
+                               fft_block, device, fft_engine)
         st = L.lib().gxc_validate_config(C.byref(self.cfg))
         if st != L.GXC_OK:
             raise ValueError(f"invalid FxKernel configuration ({L.status_name(st)})")

@@ -41,6 +41,7 @@ class FxKernel {
     int autos = 0;
     int x_engine = GXC_XENGINE_AUTO;
     int device = -1;
+    int fft_engine = GXC_FFT_AUTO;
   };
 
   /* fxkernel/src/fxkernel.h:29 */
@@ -65,6 +66,7 @@ class FxKernel {
     c.autos = opt.autos;
     c.x_engine = opt.x_engine;
     c.device = opt.device;
+    c.fft_engine = opt.fft_engine;
     cfg_ = c;
     gxc_status st = gxc_create(&c, &h);
     if (st != GXC_OK) {

@@ -56,6 +56,13 @@ enum { GXC_ROTATOR_EXACT = 0, GXC_ROTATOR_FXKERNEL = 1 };
  * TENSOR covers up to 64 antennas with FP16 data and up to 32 with FP32 data.
  * CUDA_CORE: plain FP32 FMAs.  AUTO: TENSOR when the shape fits, else CUDA_CORE. */
 enum { GXC_XENGINE_AUTO = 0, GXC_XENGINE_CUDA_CORE = 1, GXC_XENGINE_TENSOR = 2 };
+/* F-stage FFT engine.  TENSOR: the FFT as two dense DFT products on tcgen05 (FP16
+ * operands, FP32 accumulation), for FP16 / FP8 channelised output of 8192-point
+ * windows of 2-bit real data (nchan 4096); it adds four FP16 roundings inside the
+ * FFT.  CUDA_CORE: the FP32 register FFT of every shape.  AUTO: CUDA_CORE, which is
+ * the faster of the two on GB300 (16 antennas, nchan 4096, FP16: 41.1 against
+ * 44.4 ms per sub-integration). */
+enum { GXC_FFT_AUTO = 0, GXC_FFT_CUDA_CORE = 1, GXC_FFT_TENSOR = 2 };
 enum { GXC_LAYOUT_FXKERNEL = 0 };
 
 typedef struct gxc_config {
@@ -72,11 +79,12 @@ typedef struct gxc_config {
   int x_engine;    /* GXC_XENGINE_* */
   int fft_block;   /* FFTs per F/X pass; 0 = automatic */
   int device;      /* CUDA device ordinal; -1 = current device */
+  int fft_engine;  /* GXC_FFT_* */
 } gxc_config;
 
 typedef struct gxc_handle gxc_handle;
 
-/* Defaults: 2-bit real, FP32, exact rotator, autos on, automatic engine and block. */
+/* Defaults: 2-bit real, FP32, exact rotator, autos on, automatic engines and block. */
 void gxc_config_init(gxc_config *cfg);
 /* Checks a configuration without touching the GPU. */
 gxc_status gxc_validate_config(const gxc_config *cfg);

@@ -60,6 +60,12 @@ def test_validation_codes():
     assert _status(nant=4, nchan=1024, nfft=10, nbit=2, is_complex=True) == L.GXC_ERR_UNSUPPORTED
     assert _status(nant=4, nchan=1024, nfft=10, nbit=8, is_complex=True) == L.GXC_OK
     assert _status(nant=4, nchan=64, nfft=10) == L.GXC_ERR_UNSUPPORTED              # FFT below 256
+    # the tensor-core FFT: 8192-point windows of 2-bit real data with FP16 / FP8 output only
+    assert _status(nant=4, nchan=4096, nfft=10, precision="fp16", fft_engine="tensor") == L.GXC_OK
+    assert _status(nant=4, nchan=4096, nfft=10, precision="fp8", fft_engine="tensor") == L.GXC_OK
+    assert _status(nant=4, nchan=4096, nfft=10, precision="fp32", fft_engine="tensor") == L.GXC_ERR_UNSUPPORTED
+    assert _status(nant=4, nchan=2048, nfft=10, precision="fp16", fft_engine="tensor") == L.GXC_ERR_UNSUPPORTED
+    assert _status(nant=4, nchan=4096, nfft=10, precision="fp16", fft_engine=7) == L.GXC_ERR_INVALID_ARGUMENT
 
 
 def test_input_bytes_match_reference_formula():
