@@ -145,9 +145,19 @@ class FxKernel:
                 raise ValueError("odata too small")
         L.check(L.lib().gxc_accumulate(self._h, C.c_void_p(_ptr(odata))), self._h, "accumulate")
 
-    def visibilities(self) -> np.ndarray:
-        out = np.zeros((self.nbaselines, 4, self.nchan), dtype=np.complex64)
-        L.check(L.lib().gxc_get_visibilities(self._h, C.c_void_p(out.ctypes.data)), self._h, "get_visibilities")
+    def visibilities(self, out=None):
+        """The visibilities [nbl][4][nchan] complex64: a new numpy array, or copied into ``out``
+        (a preallocated C-contiguous complex64 numpy array or torch tensor, host or GPU; pinned
+        host memory reads back fastest), which is returned."""
+        if out is None:
+            out = np.zeros((self.nbaselines, 4, self.nchan), dtype=np.complex64)
+        elif isinstance(out, np.ndarray):
+            if out.dtype != np.complex64 or not out.flags.c_contiguous or out.size < self.nbaselines * 4 * self.nchan:
+                raise ValueError("out must be a C-contiguous complex64 array of nbl*4*nchan values")
+        elif hasattr(out, "numel"):
+            if out.numel() * out.element_size() < self.nbaselines * 4 * self.nchan * 8 or not out.is_contiguous():
+                raise ValueError("out must be a contiguous tensor of nbl*4*nchan complex64 values")
+        L.check(L.lib().gxc_get_visibilities(self._h, C.c_void_p(_ptr(out))), self._h, "get_visibilities")
         return out
 
     def device_visibilities_ptr(self) -> int:
