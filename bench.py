@@ -345,7 +345,8 @@ def run_batch_bench(args):
                          is_complex=w.is_complex, inputs=d["inputs"], poly=d["poly"], fso=d["fso"], autos=True))
     prec = args.precision if args.precision != "fp32" else "fp16"
     tuned = [tune(dict(b, precision=prec)) for b in base]
-    jobs16 = [dict(b, precision=prec, x_engine=t["x_engine"], fft_block=t["fft_block"]) for b, t in zip(base, tuned)]
+    jobs16 = [dict(b, precision=prec, x_engine=t["x_engine"], fft_block=t["fft_block"], fft_engine=t["fft_engine"],
+                   x_split=t["x_split"]) for b, t in zip(base, tuned)]
     jobs32 = [dict(b, precision="fp32", x_engine="cuda_core") for b in base]
     samples = sum(w.input_samples for w in ws)
     stream = torch.cuda.Stream(device=dev)
@@ -434,7 +435,9 @@ def run_batch_bench(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16", "data": "synthetic",
             "config": {"workload": CONFIGS["c3"][0], "parallelism": f"replicas x{world}",
                        "jobs": [{"nant": w.nant, "nchan": w.nchan, "nfft": w.nfft, "nbit": w.nbit,
-                                 "complex": w.is_complex, "x_engine": t["x_engine"], "fft_block": t["fft_block"]}
+                                 "complex": w.is_complex, "x_engine": t["x_engine"], "fft_block": t["fft_block"],
+                                 "fft_engine": t["fft_engine"], "x_split": t["x_split"], "tuned_ms": t["ms"],
+                                 "plans_tried": len(t["tried"])}
                                 for w, t in zip(ws, tuned)],
                        "l2": f"inputs larger than L2 ({sum(w.bytes_per_antenna * w.nant for w in ws) / 1e9:.1f} GB)"},
             "fp32_cuda_core_batch_ms": ms32, "speedup_vs_fp32_cuda_core_batch": ms32 / ms,

@@ -114,6 +114,7 @@ std::string validate(const gxc_config *c, gxc_status *st) {
   if (c->x_engine < GXC_XENGINE_AUTO || c->x_engine > GXC_XENGINE_TENSOR) return "bad x_engine";
   if (c->fft_block < 0) return "fft_block must be >= 0";
   if (c->fft_engine < GXC_FFT_AUTO || c->fft_engine > GXC_FFT_TENSOR) return "bad fft_engine";
+  if (c->x_split < GXC_XSPLIT_AUTO || c->x_split > GXC_XSPLIT_ON) return "bad x_split";
   const long long F = fft_len(c);
   if (!is_pow2(F)) return "FFT length (2*nchan real, nchan complex) must be a power of two";
   if (c->rotator == GXC_ROTATOR_FXKERNEL) {
@@ -667,7 +668,8 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
         // is <= 2^ceil(log2F/2) * 182 <= 46592 < 65504, the FP16 maximum, for every F <= 32768.
         GXC_CUDA(h,
                  launch_xstage_tensor(h->d_chan, h->chan_type, nant, c.nchan, h->T, nt, c.autos, h->d_vsum,
-                                      h->d_vcomp, s, h->log2F / 2, 2, nvis),
+                                      h->d_vcomp, s, h->log2F / 2,
+                                      c.x_split == GXC_XSPLIT_OFF ? 1 : c.x_split == GXC_XSPLIT_ON ? 3 : 2, nvis),
                  "tensor-core X-stage kernel");
       } else {
         GXC_CUDA(h,

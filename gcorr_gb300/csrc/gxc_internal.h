@@ -93,9 +93,10 @@ cudaError_t launch_xstage_cuda_core_pairs(const void *chan, int chan_type, int n
 // FP16 data: kind::f16 MMAs; FP32 data: kind::tf32 MMAs on a hi/lo split (FP32-accurate products).
 // split_e >= 0 (FP32 data whose scale is known, e.g. the F-stage's output): the FP32 path uses
 // an FP16 hi/lo split of the values times 2^-split_e; split_e < 0: the TF32 hi/lo split.
-// kparts_max = 2 with plane > 0: the FP16 / FP8 kernel may split the block's FFTs across two
-// CTAs per channel group, the second accumulating into vsum/vcomp + plane (a second plane the
-// caller allocated, zeroed and sums at the end).
+// kparts_max = 2 with plane > 0: the FP16 / FP8 kernel splits the block's FFTs across two CTAs
+// per channel group when the groups are fewer than the SMs (3: whenever the block is long enough),
+// the second CTA accumulating into vsum/vcomp + plane (a second plane the caller allocated, zeroed
+// and sums at the end).
 cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int nchan, int T, int nt, int autos,
                                  float2 *vsum, float2 *vcomp, cudaStream_t s, int split_e = -1,
                                  int kparts_max = 1, size_t plane = 0);

@@ -1310,7 +1310,7 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    if (kparts_max >= 2 && plane > 0 && nt >= 4 * KC && ngrp < nsm) {
+    if (kparts_max >= 2 && plane > 0 && nt >= 4 * KC && (ngrp < nsm || kparts_max >= 3)) {
       p.kparts = 2;
       p.kspan = (nt / 2 + KC - 1) / KC * KC;
     }

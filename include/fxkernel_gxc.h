@@ -42,6 +42,7 @@ class FxKernel {
     int x_engine = GXC_XENGINE_AUTO;
     int device = -1;
     int fft_engine = GXC_FFT_AUTO;
+    int x_split = GXC_XSPLIT_AUTO;
   };
 
   /* fxkernel/src/fxkernel.h:29 */
@@ -67,6 +68,7 @@ class FxKernel {
     c.x_engine = opt.x_engine;
     c.device = opt.device;
     c.fft_engine = opt.fft_engine;
+    c.x_split = opt.x_split;
     cfg_ = c;
     gxc_status st = gxc_create(&c, &h);
     if (st != GXC_OK) {

@@ -63,6 +63,11 @@ enum { GXC_XENGINE_AUTO = 0, GXC_XENGINE_CUDA_CORE = 1, GXC_XENGINE_TENSOR = 2 }
  * the faster of the two on GB300 (16 antennas, nchan 4096, FP16: 41.1 against
  * 44.4 ms per sub-integration). */
 enum { GXC_FFT_AUTO = 0, GXC_FFT_CUDA_CORE = 1, GXC_FFT_TENSOR = 2 };
+/* FFT-range split of the FP16 / FP8 tensor-core X-stage: each channel group's FFTs of a block go to
+ * two CTAs, the second accumulating into a second plane that finalisation adds.  AUTO: split when
+ * the channel groups are fewer than the SMs.  OFF: never.  ON: whenever the block holds at least
+ * four K chunks of FFTs (more CTAs than the groups alone give, each paying its own pipeline fill). */
+enum { GXC_XSPLIT_AUTO = 0, GXC_XSPLIT_OFF = 1, GXC_XSPLIT_ON = 2 };
 enum { GXC_LAYOUT_FXKERNEL = 0 };
 
 typedef struct gxc_config {
@@ -80,6 +85,7 @@ typedef struct gxc_config {
   int fft_block;   /* FFTs per F/X pass; 0 = automatic */
   int device;      /* CUDA device ordinal; -1 = current device */
   int fft_engine;  /* GXC_FFT_* */
+  int x_split;     /* GXC_XSPLIT_* */
 } gxc_config;
 
 typedef struct gxc_handle gxc_handle;

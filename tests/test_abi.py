@@ -66,6 +66,8 @@ def test_validation_codes():
     assert _status(nant=4, nchan=4096, nfft=10, precision="fp32", fft_engine="tensor") == L.GXC_ERR_UNSUPPORTED
     assert _status(nant=4, nchan=2048, nfft=10, precision="fp16", fft_engine="tensor") == L.GXC_ERR_UNSUPPORTED
     assert _status(nant=4, nchan=4096, nfft=10, precision="fp16", fft_engine=7) == L.GXC_ERR_INVALID_ARGUMENT
+    assert _status(nant=4, nchan=4096, nfft=10, x_split="on") == L.GXC_OK
+    assert _status(nant=4, nchan=4096, nfft=10, x_split=5) == L.GXC_ERR_INVALID_ARGUMENT
 
 
 def test_input_bytes_match_reference_formula():

@@ -58,8 +58,51 @@ def test_autotune_caches(tmp_path):
     path = str(tmp_path / "tune.json")
     r1 = tune(_job(w, d, precision="fp16"), blocks=(8, 24), path=path)
     assert r1["fft_block"] in (8, 24) and r1["x_engine"] in ("tensor", "cuda_core") and r1["tried"]
+    assert r1["fft_engine"] == "cuda_core"  # 2048-point windows: the CUDA-core FFT is the only plan
     r2 = tune(_job(w, d, precision="fp16"), blocks=(8, 24), path=path)
     assert r2 == r1
+
+
+def test_autotune_searches_f_plan_and_x_split(tmp_path):
+    """An 8192-point FP16 shape: the tuner times both F-stage plans and, for the tensor X-stage,
+    both FFT-range splits; a batch built from the tuned plan matches a single run of that plan."""
+    from gcorr_gb300.autotune import tune
+    w = synth.Workload(nant=4, nchan=4096, nfft=48, bw_hz=256e6, seed=9)
+    d = synth.random_bytes(w, device="cuda")
+    t = tune(_job(w, d, precision="fp16"), blocks=(16, 48), path=str(tmp_path / "tune.json"))
+    assert {p["fft_engine"] for p in t["tried"]} == {"cuda_core", "tensor"}
+    if t["x_engine"] == "tensor":
+        assert {p["x_split"] for p in t["tried"]} >= {"off", "on"}
+    plan = {k: t[k] for k in ("x_engine", "fft_block", "fft_engine", "x_split")}
+    b = Batch([_job(w, d, precision="fp16", **plan)])
+    b.launch()
+    fx = FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision="fp16", **plan)
+    fx.setInputData(d["inputs"])
+    fx.setDelays(d["poly"], d["fso"])
+    fx.process()
+    assert O.rel_rms(b.visibilities(0), fx.visibilities()) < 1e-6
+    fx.close()
+    b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp16", "fp8"])
+def test_x_split_modes_agree(precision):
+    """The FFT-range split only changes which CTA sums which FFTs (two accumulator planes added at
+    finalisation): forced on and off agree to FP32 rounding, counts exactly."""
+    w = synth.Workload(nant=6, nchan=1024, nfft=600, bw_hz=64e6, seed=10)
+    d = synth.random_bytes(w, device="cuda")
+    out = {}
+    for xs in ("off", "on", "auto"):
+        fx = FxKernel(w.nant, w.nchan, w.nfft, w.nbit, w.lo_hz, w.bw_hz, w.is_complex, precision=precision,
+                      x_engine="tensor", x_split=xs)
+        fx.setInputData(d["inputs"])
+        fx.setDelays(d["poly"], d["fso"])
+        fx.process()
+        out[xs] = (fx.visibilities(), fx.baseline_counts())
+        fx.close()
+    assert np.array_equal(out["on"][1], out["off"][1])
+    assert O.rel_rms(out["on"][0], out["off"][0]) < 1e-6
+    assert O.rel_rms(out["auto"][0], out["off"][0]) < 1e-6
 
 
 def test_batch_on_pinned_host_inputs():
