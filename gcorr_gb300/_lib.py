@@ -22,6 +22,7 @@ GXC_ROTATOR_EXACT, GXC_ROTATOR_FXKERNEL = 0, 1
 GXC_XENGINE_AUTO, GXC_XENGINE_CUDA_CORE, GXC_XENGINE_TENSOR = 0, 1, 2
 GXC_FFT_AUTO, GXC_FFT_CUDA_CORE, GXC_FFT_TENSOR = 0, 1, 2
 GXC_XSPLIT_AUTO, GXC_XSPLIT_OFF, GXC_XSPLIT_ON = 0, 1, 2
+GXC_FP8_SCALE_CHANNEL, GXC_FP8_SCALE_HANDLE = 0, 1
 _STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "out of memory",
            5: "bad call order", 6: "device wait timed out", 7: "end of data"}
 
@@ -47,7 +48,7 @@ class GxcConfig(C.Structure):
     _fields_ = [("nant", C.c_int), ("nchan", C.c_int), ("nfft", C.c_int), ("nbit", C.c_int),
                 ("is_complex", C.c_int), ("lo_hz", C.c_double), ("bw_hz", C.c_double), ("precision", C.c_int),
                 ("rotator", C.c_int), ("autos", C.c_int), ("x_engine", C.c_int), ("fft_block", C.c_int),
-                ("device", C.c_int), ("fft_engine", C.c_int), ("x_split", C.c_int)]
+                ("device", C.c_int), ("fft_engine", C.c_int), ("x_split", C.c_int), ("fp8_scaling", C.c_int)]
 
 
 class GxcVdifHeader(C.Structure):

@@ -14,10 +14,10 @@ class Batch:
     """jobs: sequence of dicts with keys ``inputs`` (device tensors / addresses, one per
     antenna), ``poly`` [nant,3], ``fso`` [nant] and the FxKernel configuration keys
     (nant, nchan, nfft, nbit, lo, bw, is_complex, precision, rotator, autos,
-    x_engine, fft_block, fft_engine, x_split)."""
+    x_engine, fft_block, fft_engine, x_split, fp8_scaling)."""
 
     CFG_KEYS = ("nant", "nchan", "nfft", "nbit", "lo", "bw", "is_complex", "precision", "rotator", "autos",
-                "x_engine", "fft_block", "fft_engine", "x_split")
+                "x_engine", "fft_block", "fft_engine", "x_split", "fp8_scaling")
 
     def __init__(self, jobs: Sequence[dict]):
         self._keep = []

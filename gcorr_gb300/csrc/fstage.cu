@@ -159,9 +159,9 @@ cudaError_t make_twiddles(int F, float2 **out) {
 int fstage_supported(int F) { return F >= 256 && F <= 32768 && (F & (F - 1)) == 0; }
 
 cudaError_t launch_fstage(const Job &job, const float2 *twiddles, int t0, int nt, int T, void *chan, int chan_type,
-                          float out_scale, cudaStream_t s) {
+                          float out_scale, cudaStream_t s, const float *cscale) {
   if (nt <= 0) return cudaSuccess;
-  const FParams prm = fstage_params(job, twiddles, t0, T, chan, out_scale, nullptr);
+  const FParams prm = fstage_params(job, twiddles, t0, T, chan, out_scale, nullptr, cscale);
   if (chan_type == CHAN_F32) {
     return job.is_complex ? launch_fstage_l<float2, true>(prm, nt, s) : launch_fstage_l<float2, false>(prm, nt, s);
   }

@@ -147,7 +147,18 @@ struct FParams {
   int sub_shift, sub_mask;    // substride = 1 << sub_shift
   int fsub_shift, fsub_mask;  // fsub = 1 << fsub_shift
   float2 *probe;              // DBG kernels: decoded samples [nant][2][nfft][F] before rotation
+  const float *cscale;        // FP8 output: per-channel scale [nchan] (replaces out_scale), or null
 };
+
+// Output scale of channel c: FP8 output with per-channel scales uses cscale[c] (the caller then
+// passes base = 1, or the kernel's own exact internal factor), every other case base.
+template <typename OutT>
+__device__ __forceinline__ float chan_scale(const float *cscale, int c, float base) {
+  if constexpr (std::is_same<OutT, __nv_fp8x2_e4m3>::value) {
+    if (cscale) return base * __ldg(&cscale[c]);
+  }
+  return base;
+}
 
 // float2 entries that follow the F-point twiddle table when F = 8192 (make_twiddles).
 constexpr int kPairTw1 = 16 * 16, kPairTw2 = 16 * 256;
@@ -160,7 +171,7 @@ inline int fparams_ilog2(int x) {
 
 // Launch parameters of FFTs [t0, t0 + nt) of a block of T (twiddles from make_twiddles).
 inline FParams fstage_params(const Job &job, const float2 *twiddles, int t0, int T, void *chan, float out_scale,
-                             float2 *probe) {
+                             float2 *probe, const float *cscale = nullptr) {
   FParams prm;
   prm.job = job;
   prm.tw = twiddles;
@@ -175,6 +186,7 @@ inline FParams fstage_params(const Job &job, const float2 *twiddles, int t0, int
   prm.fsub_shift = fparams_ilog2(job.fsub);
   prm.fsub_mask = job.fsub - 1;
   prm.probe = probe;
+  prm.cscale = cscale;
   return prm;
 }
 
@@ -442,7 +454,7 @@ __global__ void __launch_bounds__(FPlan<L, CPLX>::NT, FPlan<L, CPLX>::MINB) fsta
         float2 fr;
         if constexpr (NB % FSUB == 0) fr = cmul(fs, fstept[(iv / FSUB) + r * (NB / FSUB)]);
         else fr = cmul(fsubt[c & (FSUB - 1)], fstept[c / FSUB]);
-        o[(size_t)r * (NB / 16) * ctile_stride] = to_out<OutT>(cmul(v[r], fr), prm.out_scale);
+        o[(size_t)r * (NB / 16) * ctile_stride] = to_out<OutT>(cmul(v[r], fr), chan_scale<OutT>(prm.cscale, c, prm.out_scale));
       }
     }
   }
@@ -740,8 +752,16 @@ __global__ void __launch_bounds__(256, 2) fstage_pair_kernel(FParams prm) {
 #pragma unroll
     for (int r = 0; r < RKEEP; r++) {
       const float2 fst = fstept[(2 * iv) / FSUB + r * (2 * NB / FSUB)];
-      const float2 a = cmul(make_float2(u[r].re.x, u[r].im.x), cmul(fsA, fst));
-      const float2 b = cmul(make_float2(u[r].re.y, u[r].im.y), cmul(fsB, fst));
+      float2 a = cmul(make_float2(u[r].re.x, u[r].im.x), cmul(fsA, fst));
+      float2 b = cmul(make_float2(u[r].re.y, u[r].im.y), cmul(fsB, fst));
+      if constexpr (std::is_same<OutT, __nv_fp8x2_e4m3>::value) {
+        if (prm.cscale) {  // channels 2 iv + 2 NB r and the next one
+          const int c = 2 * iv + r * 2 * NB;
+          const float sa = __ldg(&prm.cscale[c]), sb = __ldg(&prm.cscale[c + 1]);
+          a = make_float2(a.x * sa, a.y * sa);
+          b = make_float2(b.x * sb, b.y * sb);
+        }
+      }
       store_pair<OutT>(o + (size_t)r * (2 * NB / 16) * ctile_stride, a, b);
     }
   }
@@ -990,7 +1010,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(512, 1) fstage_clust
     for (int r = 0; r < RKEEP; r++) {
       const int c = k1 + 128 * (ivd + 16 * r);
       const float2 fr = cmul(fsubt[c & (FSUB - 1)], fstept[c / FSUB]);
-      out0[(size_t)(c >> 4) * ctile_stride + (c & 15)] = to_out<OutT>(cmul(v[r], fr), prm.out_scale);
+      out0[(size_t)(c >> 4) * ctile_stride + (c & 15)] =
+          to_out<OutT>(cmul(v[r], fr), chan_scale<OutT>(prm.cscale, c, prm.out_scale));
     }
   }
 }
@@ -1185,7 +1206,8 @@ __global__ void __launch_bounds__(HPlan<L>::NT, HPlan<L>::MINB) fstage_h_kernel(
 #pragma unroll
     for (int r = 0; r < RKEEP; r++) {
       const float2 fr = cmul(fs, fstept[(iv / FSUB) + r * (NBL / FSUB)]);
-      o[(size_t)r * (NBL / 16) * ctile_stride] = to_out<OutT>(cmul(v[r], fr), oscale);
+      o[(size_t)r * (NBL / 16) * ctile_stride] =
+          to_out<OutT>(cmul(v[r], fr), chan_scale<OutT>(prm.cscale, iv + r * NBL, oscale));
     }
   }
 }

@@ -74,6 +74,7 @@ struct Params {
   int t0, nt, T;
   void *chan;
   float out_scale;
+  const float *cscale;  // FP8 output: per-channel scale [nchan] (replaces out_scale), or null
   int *err;
 };
 
@@ -329,7 +330,7 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
           const int k2 = (col0 >> 1) + e, k = k1 + 64 * k2;
           const float2 fr = cmul(fs, fstept[k2]);
           const float2 z = cmul(make_float2(v[2 * e], v[2 * e + 1]), fr);
-          o[(size_t)(k >> 4) * ctile_stride] = to_out<OutT>(z, sc);
+          o[(size_t)(k >> 4) * ctile_stride] = to_out<OutT>(z, chan_scale<OutT>(p.cscale, k, sc));
         }
       }
     }
@@ -403,7 +404,7 @@ cudaError_t make_fstage_tc_tables(void **out) {
 }
 
 cudaError_t launch_fstage_tc(const Job &job, const void *tables, int t0, int nt, int T, void *chan, int chan_type,
-                             float out_scale, cudaStream_t s) {
+                             float out_scale, cudaStream_t s, const float *cscale) {
   using namespace ftc;
   if (nt <= 0) return cudaSuccess;
   if (!fstage_tc_supported(job, chan_type) || !tables) return cudaErrorInvalidValue;
@@ -415,6 +416,7 @@ cudaError_t launch_fstage_tc(const Job &job, const void *tables, int t0, int nt,
   p.T = T;
   p.chan = chan;
   p.out_scale = out_scale;
+  p.cscale = cscale;
   cudaError_t e = cudaGetSymbolAddress((void **)&p.err, g_ftc_err);
   if (e != cudaSuccess) return e;
   int dev = 0, nsm = 0;

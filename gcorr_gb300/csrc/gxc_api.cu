@@ -28,6 +28,11 @@ struct gxc_handle {
   void *d_tc_tables = nullptr;
   float out_scale = 1.f;   // applied to channelised values before the cast
   float vis_scale = 1.f;   // 1/out_scale^2, applied at finalisation
+  // FP8 per-channel scales (GXC_FP8_SCALE_CHANNEL): calibration block of cal_T FFTs in FP32,
+  // per-channel output scale and its inverse square
+  int cal_T = 0;
+  float2 *d_cal = nullptr;
+  float *d_cscale = nullptr, *d_cvscale = nullptr;
   size_t bytes_per_ant = 0;
 
   // inputs
@@ -115,6 +120,7 @@ std::string validate(const gxc_config *c, gxc_status *st) {
   if (c->fft_block < 0) return "fft_block must be >= 0";
   if (c->fft_engine < GXC_FFT_AUTO || c->fft_engine > GXC_FFT_TENSOR) return "bad fft_engine";
   if (c->x_split < GXC_XSPLIT_AUTO || c->x_split > GXC_XSPLIT_ON) return "bad x_split";
+  if (c->fp8_scaling < GXC_FP8_SCALE_CHANNEL || c->fp8_scaling > GXC_FP8_SCALE_HANDLE) return "bad fp8_scaling";
   const long long F = fft_len(c);
   if (!is_pow2(F)) return "FFT length (2*nchan real, nchan complex) must be a power of two";
   if (c->rotator == GXC_ROTATOR_FXKERNEL) {
@@ -242,6 +248,9 @@ static void release(gxc_handle *h) {
   cudaFree(h->d_valid);
   cudaFree(h->d_tw);
   cudaFree(h->d_tc_tables);
+  cudaFree(h->d_cal);
+  cudaFree(h->d_cscale);
+  cudaFree(h->d_cvscale);
   cudaFree(h->d_pairs);
   cudaFree(h->d_chan);
   cudaFree(h->d_vsum);
@@ -373,6 +382,18 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   // faster (16 antennas, nchan 4096, FP16: F-stage 41.1 ms against 44.4 ms per sub-integration)
   h->tc_fstage = cfg->fft_engine == GXC_FFT_TENSOR && fstage_tc_supported(j, h->chan_type);
   if (e == cudaSuccess && h->tc_fstage) e = make_fstage_tc_tables(&h->d_tc_tables);
+  if (h->chan_type == CHAN_F8 && cfg->fp8_scaling == GXC_FP8_SCALE_CHANNEL) {
+    // calibration block: up to 64 FFTs, at most 256 MB of FP32 channelised data (at least 4 FFTs)
+    const size_t per_fft32 = (size_t)cfg->nchan * 2 * nant * sizeof(float2);
+    size_t ct = ((size_t)256 << 20) / per_fft32;
+    if (ct > 64) ct = 64;
+    if (ct < 4) ct = 4;
+    if (ct > (size_t)cfg->nfft) ct = (size_t)cfg->nfft;
+    h->cal_T = (int)ct;
+    A((void **)&h->d_cal, per_fft32 * ct);
+    A((void **)&h->d_cscale, sizeof(float) * cfg->nchan);
+    A((void **)&h->d_cvscale, sizeof(float) * cfg->nchan);
+  }
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_done, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMemset(h->d_vis, 0, sizeof(float2) * nvis);
   if (e != cudaSuccess) {
@@ -498,11 +519,59 @@ gxc_status gxc_set_delays(gxc_handle *h, const double *poly, const double *fso) 
   return GXC_OK;
 }
 
+// FP8 per-channel scales from the calibration block cal [ctile][t < nt][stream][16] (FP32 spectra):
+// one CTA per 16-channel tile; channel c's RMS over the nonzero values of all FFTs and streams
+// (flagged FFTs hold zeros), scale 2^e with e = floor(log2(4 / rms)) so the RMS lands in [2, 4),
+// clamped to [-60, 60]; a channel with no data keeps the handle's exponent def_e.  vscale = 2^-2e.
+__global__ void chan_scales_kernel(const float2 *__restrict__ cal, int nstream, int nchan, int nt, int def_e,
+                                   float *__restrict__ cscale, float *__restrict__ cvscale) {
+  const int tile = blockIdx.x, ci = threadIdx.x & 15, j = threadIdx.x >> 4;  // 16 x 16 threads
+  const int n = nt * nstream;
+  const float2 *base = cal + (size_t)tile * n * 16;
+  double acc = 0.0;
+  int cnt = 0;
+  for (int i = j; i < n; i += 16) {
+    const float2 v = base[(size_t)i * 16 + ci];
+    const double p = (double)v.x * v.x + (double)v.y * v.y;
+    acc += p;
+    cnt += p > 0.0 ? 1 : 0;
+  }
+  __shared__ double sacc[16][17];
+  __shared__ int scnt[16][17];
+  sacc[j][ci] = acc;
+  scnt[j][ci] = cnt;
+  __syncthreads();
+  if (j == 0) {
+    for (int k = 1; k < 16; k++) {
+      acc += sacc[k][ci];
+      cnt += scnt[k][ci];
+    }
+    int e = def_e;
+    if (cnt > 0 && acc > 0.0 && isfinite(acc)) {
+      const double rms = sqrt(acc / cnt);
+      e = (int)floor(log2(4.0 / rms));
+      e = e < -60 ? -60 : e > 60 ? 60 : e;
+    }
+    const int c = tile * 16 + ci;
+    if (c < nchan) {
+      cscale[c] = ldexpf(1.0f, e);
+      cvscale[c] = ldexpf(1.0f, -2 * e);
+    }
+  }
+}
+
+static cudaError_t launch_chan_scales(const float2 *cal, int nstream, int nchan, int nt, int def_e, float *cscale,
+                                      float *cvscale, cudaStream_t s) {
+  chan_scales_kernel<<<(unsigned)((nchan + 15) / 16), 256, 0, s>>>(cal, nstream, nchan, nt, def_e, cscale, cvscale);
+  return cudaGetLastError();
+}
+
 // finalisation: vis = (sum + comp) * scale / count (fxkernel.cpp:358-367)
 // Sums the two accumulator planes (i and i + n) with a compensated add; a plane no launch wrote
 // is zero and leaves the result bit-identical to the first plane's.
 __global__ void finalize_kernel(const float2 *__restrict__ vsum, const float2 *__restrict__ vcomp,
                                 const int32_t *__restrict__ counts, int nchan, size_t n, float scale,
+                                const float *__restrict__ chan_vscale,
                                 float2 *__restrict__ vis) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -512,7 +581,8 @@ __global__ void finalize_kernel(const float2 *__restrict__ vsum, const float2 *_
   float sx = s0.x, ex = c0.x, sy = s0.y, ey = c0.y;
   two_sum_add(sx, ex, s1.x);
   two_sum_add(sy, ey, s1.y);
-  float re = (sx + (ex + c1.x)) * scale, im = (sy + (ey + c1.y)) * scale;
+  const float sc = chan_vscale ? chan_vscale[i % nchan] : scale;
+  float re = (sx + (ex + c1.x)) * sc, im = (sy + (ey + c1.y)) * sc;
   if (cnt > 0) {
     re /= (float)cnt;
     im /= (float)cnt;
@@ -652,12 +722,25 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
         waited = j;
       }
     }
+    if (b == 0 && h->d_cscale) {
+      // FP8 per-channel scales: the first cal_T FFTs channelised in FP32, each channel's RMS over
+      // them and all streams, a power of two per channel
+      GXC_CUDA(h, launch_fstage(h->job, h->d_tw, 0, h->cal_T, h->cal_T, h->d_cal, CHAN_F32, 1.0f, s),
+               "F-stage calibration kernel");
+      GXC_CUDA(h, launch_chan_scales(h->d_cal, 2 * nant, c.nchan, h->cal_T, -ilog2i(h->F) / 2 - (c.is_complex ? 4 : 0),
+                                     h->d_cscale, h->d_cvscale, s),
+               "channel scale kernel");
+      launches += 2;
+    }
+    // with per-channel FP8 scales the channel's scale replaces the handle's
+    const float osc = h->d_cscale ? 1.0f : h->out_scale;
     if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b], s), "timing event");
     if (h->tc_fstage)
-      GXC_CUDA(h, launch_fstage_tc(h->job, h->d_tc_tables, t0, nt, h->T, h->d_chan, h->chan_type, h->out_scale, s),
+      GXC_CUDA(h, launch_fstage_tc(h->job, h->d_tc_tables, t0, nt, h->T, h->d_chan, h->chan_type, osc, s,
+                                   h->d_cscale),
                "tensor-core F-stage kernel");
     else
-      GXC_CUDA(h, launch_fstage(h->job, h->d_tw, t0, nt, h->T, h->d_chan, h->chan_type, h->out_scale, s),
+      GXC_CUDA(h, launch_fstage(h->job, h->d_tw, t0, nt, h->T, h->d_chan, h->chan_type, osc, s, h->d_cscale),
                "F-stage kernel");
     launches++;
     if (timing) GXC_CUDA(h, cudaEventRecord(h->ev_stage[3 * b + 1], s), "timing event");
@@ -686,7 +769,7 @@ extern "C++" gxc_status gxc::process_chained(gxc_handle *h, void *stream, cudaEv
   if (nvis > 0) {
     const int th = 256;
     finalize_kernel<<<(unsigned)((nvis + th - 1) / th), th, 0, s>>>(h->d_vsum, h->d_vcomp, h->d_counts, c.nchan,
-                                                                     nvis, h->vis_scale, h->d_vis);
+                                                                     nvis, h->vis_scale, h->d_cvscale, h->d_vis);
     GXC_CUDA(h, cudaGetLastError(), "finalize kernel");
     launches++;
   }

@@ -62,8 +62,9 @@ inline int chan_type_of(int precision) {
 cudaError_t launch_geometry(const Job &job, cudaStream_t s);
 cudaError_t launch_counts(const Job &job, int autos, int32_t *counts, uint8_t *valid_flags, cudaStream_t s);
 cudaError_t make_twiddles(int F, float2 **out);
+// cscale (FP8 output only): per-channel output scale [nchan] replacing out_scale, or null.
 cudaError_t launch_fstage(const Job &job, const float2 *twiddles, int t0, int nt, int T, void *chan, int chan_type,
-                          float out_scale, cudaStream_t s);
+                          float out_scale, cudaStream_t s, const float *cscale = nullptr);
 int fstage_supported(int F);
 // fstage_probe.cu: the F-stage of FFTs [t0, t0+nt) with every decoded input sample also written to
 // probe [nant][2][nfft][F] (complex float) before the fringe rotation.  chan must hold T FFTs of
@@ -75,7 +76,7 @@ cudaError_t launch_fstage_probe(const Job &job, const float2 *twiddles, int t0, 
 int fstage_tc_supported(const Job &job, int chan_type);
 cudaError_t make_fstage_tc_tables(void **out);  // its constant operands (cudaMalloc'd; caller frees)
 cudaError_t launch_fstage_tc(const Job &job, const void *tables, int t0, int nt, int T, void *chan, int chan_type,
-                             float out_scale, cudaStream_t s);
+                             float out_scale, cudaStream_t s, const float *cscale = nullptr);
 cudaError_t fstage_tc_take_error(int *flag);
 
 // xstage_fp32.cu: accumulates visibilities of FFTs [0, nt) of the block into

@@ -22,11 +22,12 @@ ROTATOR = {"exact": L.GXC_ROTATOR_EXACT, "fxkernel": L.GXC_ROTATOR_FXKERNEL}
 XENGINE = {"auto": L.GXC_XENGINE_AUTO, "cuda_core": L.GXC_XENGINE_CUDA_CORE, "tensor": L.GXC_XENGINE_TENSOR}
 FFTENGINE = {"auto": L.GXC_FFT_AUTO, "cuda_core": L.GXC_FFT_CUDA_CORE, "tensor": L.GXC_FFT_TENSOR}
 XSPLIT = {"auto": L.GXC_XSPLIT_AUTO, "off": L.GXC_XSPLIT_OFF, "on": L.GXC_XSPLIT_ON}
+FP8SCALE = {"channel": L.GXC_FP8_SCALE_CHANNEL, "handle": L.GXC_FP8_SCALE_HANDLE}
 
 
 def make_config(nant, nchan, nfft, nbit=2, lo=8.4e9, bw=64e6, is_complex=False, precision="fp32",
                 rotator="exact", autos=True, x_engine="auto", fft_block=0, device=-1,
-                fft_engine="auto", x_split="auto") -> L.GxcConfig:
+                fft_engine="auto", x_split="auto", fp8_scaling="channel") -> L.GxcConfig:
     cfg = L.GxcConfig()
     L.lib().gxc_config_init(C.byref(cfg))
     cfg.nant, cfg.nchan, cfg.nfft, cfg.nbit = int(nant), int(nchan), int(nfft), int(nbit)
@@ -40,6 +41,7 @@ def make_config(nant, nchan, nfft, nbit=2, lo=8.4e9, bw=64e6, is_complex=False, 
     cfg.device = int(device)
     cfg.fft_engine = FFTENGINE[fft_engine] if isinstance(fft_engine, str) else int(fft_engine)
     cfg.x_split = XSPLIT[x_split] if isinstance(x_split, str) else int(x_split)
+    cfg.fp8_scaling = FP8SCALE[fp8_scaling] if isinstance(fp8_scaling, str) else int(fp8_scaling)
     return cfg
 
 
@@ -59,9 +61,10 @@ class FxKernel:
 
     def __init__(self, nant: int, nchan: int, nfft: int, nbit: int, lo: float, bw: float, is_complex: bool = False,
                  *, precision: str = "fp32", rotator: str = "exact", autos: bool = True, x_engine: str = "auto",
-                 fft_block: int = 0, device: int = -1, fft_engine: str = "auto", x_split: str = "auto"):
+                 fft_block: int = 0, device: int = -1, fft_engine: str = "auto", x_split: str = "auto",
+                 fp8_scaling: str = "channel"):
         self.cfg = make_config(nant, nchan, nfft, nbit, lo, bw, is_complex, precision, rotator, autos, x_engine,
-                               fft_block, device, fft_engine, x_split)
+                               fft_block, device, fft_engine, x_split, fp8_scaling)
         st = L.lib().gxc_validate_config(C.byref(self.cfg))
         if st != L.GXC_OK:
             raise ValueError(f"invalid FxKernel configuration ({L.status_name(st)})")

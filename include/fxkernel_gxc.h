@@ -43,6 +43,7 @@ class FxKernel {
     int device = -1;
     int fft_engine = GXC_FFT_AUTO;
     int x_split = GXC_XSPLIT_AUTO;
+    int fp8_scaling = GXC_FP8_SCALE_CHANNEL;
   };
 
   /* fxkernel/src/fxkernel.h:29 */
@@ -69,6 +70,7 @@ class FxKernel {
     c.device = opt.device;
     c.fft_engine = opt.fft_engine;
     c.x_split = opt.x_split;
+    c.fp8_scaling = opt.fp8_scaling;
     cfg_ = c;
     gxc_status st = gxc_create(&c, &h);
     if (st != GXC_OK) {

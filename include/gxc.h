@@ -68,6 +68,13 @@ enum { GXC_FFT_AUTO = 0, GXC_FFT_CUDA_CORE = 1, GXC_FFT_TENSOR = 2 };
  * the channel groups are fewer than the SMs.  OFF: never.  ON: whenever the block holds at least
  * four K chunks of FFTs (more CTAs than the groups alone give, each paying its own pipeline fill). */
 enum { GXC_XSPLIT_AUTO = 0, GXC_XSPLIT_OFF = 1, GXC_XSPLIT_ON = 2 };
+/* Scaling of FP8 (E4M3) channelised data.  CHANNEL: every process() first channelises its first
+ * few FFTs in FP32 (up to 64, fewer for very large arrays), measures each channel's RMS over those
+ * FFTs and all streams, and casts each channel with its own power of two that puts that RMS near 4
+ * (E4M3's largest finite value is 448); finalisation divides each channel by its scale squared,
+ * exactly.  A band with a steep bandpass keeps every channel in E4M3's normal range.  HANDLE: one
+ * power of two for every channel, from the FFT length and the sample format. */
+enum { GXC_FP8_SCALE_CHANNEL = 0, GXC_FP8_SCALE_HANDLE = 1 };
 enum { GXC_LAYOUT_FXKERNEL = 0 };
 
 typedef struct gxc_config {
@@ -86,6 +93,7 @@ typedef struct gxc_config {
   int device;      /* CUDA device ordinal; -1 = current device */
   int fft_engine;  /* GXC_FFT_* */
   int x_split;     /* GXC_XSPLIT_* */
+  int fp8_scaling; /* GXC_FP8_SCALE_* (FP8 precision only) */
 } gxc_config;
 
 typedef struct gxc_handle gxc_handle;

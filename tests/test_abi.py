@@ -68,6 +68,8 @@ def test_validation_codes():
     assert _status(nant=4, nchan=4096, nfft=10, precision="fp16", fft_engine=7) == L.GXC_ERR_INVALID_ARGUMENT
     assert _status(nant=4, nchan=4096, nfft=10, x_split="on") == L.GXC_OK
     assert _status(nant=4, nchan=4096, nfft=10, x_split=5) == L.GXC_ERR_INVALID_ARGUMENT
+    assert _status(nant=4, nchan=4096, nfft=10, precision="fp8", fp8_scaling="handle") == L.GXC_OK
+    assert _status(nant=4, nchan=4096, nfft=10, precision="fp8", fp8_scaling=3) == L.GXC_ERR_INVALID_ARGUMENT
 
 
 def test_input_bytes_match_reference_formula():
