@@ -81,6 +81,30 @@ struct Params {
   size_t plane;
 };
 
+// Adds val[i] into the compensated accumulators (vsum, vcomp) at off[i], for every i < N with
+// use[i].  All loads of the batch are issued before its first store, so their latencies overlap
+// (one load-add-store at a time waited a full memory round trip per output: in the FP16
+// X-stage that was about a quarter of each CTA's time).
+template <int N>
+__device__ __forceinline__ void rmw_batch(float2 *vsum, float2 *vcomp, const size_t (&off)[N],
+                                          const float2 (&val)[N], const bool (&use)[N]) {
+  float2 sm[N], e[N];
+#pragma unroll
+  for (int i = 0; i < N; i++)
+    if (use[i]) {
+      sm[i] = vsum[off[i]];
+      e[i] = vcomp[off[i]];
+    }
+#pragma unroll
+  for (int i = 0; i < N; i++)
+    if (use[i]) {
+      two_sum_add(sm[i].x, e[i].x, val[i].x);
+      two_sum_add(sm[i].y, e[i].y, val[i].y);
+      vsum[off[i]] = sm[i];
+      vcomp[off[i]] = e[i];
+    }
+}
+
 // FP16 and FP8 paths: one accumulation over the whole FFT block (its TMEM rounding
 // bias, ~1e-5 over 2048 FFTs, is far below the FP16 / FP8 quantisation error).
 // A 128-byte SW128 row holds 64 FFTs of FP16 or 128 FFTs of FP8 (E4M3) values;
@@ -317,38 +341,47 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
       const int j = s1 >> 1, l = s1 & 1;
       for (int G = 0; G < NG; G++) {
         const int c = cb + G * p.g + my_gi;
-        for (int pc = 0; pc < clen; pc += 16) {
-          __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skip below
-          const int col = col0 + pc;
-          float v[16], pv[16];
-          tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(G * 128 + col), v);
+        // up to two 16-column pieces (8 outputs) per accumulator batch
+        for (int pc0 = 0; pc0 < clen; pc0 += 32) {
+          size_t off[8];
+          float2 val[8];
+          bool use[8];
 #pragma unroll
-          for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
-          if (col < my_gi * p.R || col >= (my_gi + 1) * p.R || s1 >= n) continue;
-          const int s2b = (col - my_gi * p.R) >> 1;
+          for (int u = 0; u < 2; u++) {
 #pragma unroll
-          for (int qq = 0; qq < 4; qq++) {
-            const int q = qq + 4 * part1;
-            const int s2 = s2b + q;
-            if (s2 >= n) continue;
-            const int k = s2 >> 1, m = s2 & 1;
-            if (j > k || (j == k && !p.autos)) continue;
-            float re, im;
-            if (part1 == 0) {
-              re = v[2 * q] + pv[2 * q + 1];
-              im = pv[2 * q] - v[2 * q + 1];
-            } else {
-              re = pv[2 * q] + v[2 * q + 1];
-              im = v[2 * q] - pv[2 * q + 1];
+            for (int qq = 0; qq < 4; qq++) use[4 * u + qq] = false;
+            const int pc = pc0 + 16 * u;
+            if (pc >= clen) continue;  // the same for the whole warp
+            __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skip below
+            const int col = col0 + pc;
+            float v[16], pv[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(G * 128 + col), v);
+#pragma unroll
+            for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
+            if (col < my_gi * p.R || col >= (my_gi + 1) * p.R || s1 >= n) continue;
+            const int s2b = (col - my_gi * p.R) >> 1;
+#pragma unroll
+            for (int qq = 0; qq < 4; qq++) {
+              const int q = qq + 4 * part1;
+              const int s2 = s2b + q;
+              if (s2 >= n) continue;
+              const int k = s2 >> 1, m = s2 & 1;
+              if (j > k || (j == k && !p.autos)) continue;
+              float re, im;
+              if (part1 == 0) {
+                re = v[2 * q] + pv[2 * q + 1];
+                im = pv[2 * q] - v[2 * q + 1];
+              } else {
+                re = pv[2 * q] + v[2 * q + 1];
+                im = v[2 * q] - pv[2 * q + 1];
+              }
+              const int bl = baseline_index(j, k, p.nant);
+              use[4 * u + qq] = true;
+              val[4 * u + qq] = make_float2(re, im);
+              off[4 * u + qq] = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
             }
-            const int bl = baseline_index(j, k, p.nant);
-            const size_t o = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
-            float2 sm = vsum[o], e = vcomp[o];
-            two_sum_add(sm.x, e.x, re);
-            two_sum_add(sm.y, e.y, im);
-            vsum[o] = sm;
-            vcomp[o] = e;
           }
+          rmw_batch<8>(vsum, vcomp, off, val, use);
         }
       }
     }
@@ -670,21 +703,24 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
       for (int G = 0; G < NG; G++) {
         const int c = cb + G * GCH + my_gi;
 #pragma unroll
-        for (int a = 0; a < PP; a++) {
+        for (int a = 0; a < PP; a++) {  // one accumulator batch of 4 outputs per piece
+          size_t off[4];
+          float2 val[4];
+          bool use[4];
 #pragma unroll
           for (int qq = 0; qq < 4; qq++) {
+            use[qq] = false;
             const int s2 = 8 * a + qq + 4 * part1;
             if (s2 >= n) continue;
             const int k = s2 >> 1, m = s2 & 1;
             if (j > k || (j == k && !p.autos)) continue;
             const int bl = baseline_index(j, k, p.nant);
-            const size_t o = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
-            float2 sm = p.vsum[o], e = p.vcomp[o];
-            two_sum_add(sm.x, e.x, acc[G][a][qq].x * p.split_unsc);  // exact: a power of two
-            two_sum_add(sm.y, e.y, acc[G][a][qq].y * p.split_unsc);
-            p.vsum[o] = sm;
-            p.vcomp[o] = e;
+            use[qq] = true;
+            off[qq] = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
+            // the Gram sums times split_unsc: exact, a power of two
+            val[qq] = make_float2(acc[G][a][qq].x * p.split_unsc, acc[G][a][qq].y * p.split_unsc);
           }
+          rmw_batch<4>(p.vsum, p.vcomp, off, val, use);
         }
       }
     }
