@@ -1024,37 +1024,45 @@ __device__ __forceinline__ void big2_epilogue(const Params &p, uint32_t tmem, in
   const int arow = 32 * warp + lane;
   const int s1 = s_lo + (arow >> 1), part1 = arow & 1;
   const int j = s1 >> 1, l = s1 & 1;
-  for (int pc = 0; pc < npc; pc++) {
-    __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skips below
-    float v[16], pv[16];
-    tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + col0 + 16u * pc, v);
+  // one 16-column piece (4 outputs) per accumulator batch
+  for (int pc0 = 0; pc0 < npc; pc0++) {
+    size_t off[4];
+    float2 val[4];
+    bool use[4];
 #pragma unroll
-    for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
-    if (s1 >= n) continue;
-    const int s2b = s2_lo + 8 * pc;
+    for (int u = 0; u < 1; u++) {
+      const int pc = pc0 + u;
 #pragma unroll
-    for (int qq = 0; qq < 4; qq++) {
-      const int q = qq + 4 * part1;
-      const int s2 = s2b + q;
-      if (s2 >= n) continue;
-      const int k = s2 >> 1, m = s2 & 1;
-      if (j > k || (j == k && !p.autos)) continue;
-      float re, im;
-      if (part1 == 0) {
-        re = v[2 * q] + pv[2 * q + 1];
-        im = pv[2 * q] - v[2 * q + 1];
-      } else {
-        re = pv[2 * q] + v[2 * q + 1];
-        im = v[2 * q] - pv[2 * q + 1];
+      for (int qq = 0; qq < 4; qq++) use[4 * u + qq] = false;
+      __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skips below
+      float v[16], pv[16];
+      tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + col0 + 16u * pc, v);
+#pragma unroll
+      for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
+      if (s1 >= n) continue;
+      const int s2b = s2_lo + 8 * pc;
+#pragma unroll
+      for (int qq = 0; qq < 4; qq++) {
+        const int q = qq + 4 * part1;
+        const int s2 = s2b + q;
+        if (s2 >= n) continue;
+        const int k = s2 >> 1, m = s2 & 1;
+        if (j > k || (j == k && !p.autos)) continue;
+        float re, im;
+        if (part1 == 0) {
+          re = v[2 * q] + pv[2 * q + 1];
+          im = pv[2 * q] - v[2 * q + 1];
+        } else {
+          re = pv[2 * q] + v[2 * q + 1];
+          im = v[2 * q] - pv[2 * q + 1];
+        }
+        const int bl = baseline_index(j, k, p.nant);
+        use[4 * u + qq] = true;
+        val[4 * u + qq] = make_float2(re, im);
+        off[4 * u + qq] = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
       }
-      const int bl = baseline_index(j, k, p.nant);
-      const size_t o = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
-      float2 sm = p.vsum[o], e = p.vcomp[o];
-      two_sum_add(sm.x, e.x, re);
-      two_sum_add(sm.y, e.y, im);
-      p.vsum[o] = sm;
-      p.vcomp[o] = e;
     }
+    rmw_batch<4>(p.vsum, p.vcomp, off, val, use);
   }
 }
 
