@@ -79,6 +79,9 @@ struct Params {
   // accumulating into plane `part` of vsum/vcomp (planes `plane` elements apart)
   int kparts, kspan;
   size_t plane;
+  // FP16 / FP8 kernel: persist = 1 runs one CTA per SM over equal shares of all (group, chunk)
+  // units; ngrp = channel groups of the launch
+  int persist, ngrp;
 };
 
 // Adds val[i] into the compensated accumulators (vsum, vcomp) at off[i], for every i < N with
@@ -105,10 +108,56 @@ __device__ __forceinline__ void rmw_batch(float2 *vsum, float2 *vcomp, const siz
     }
 }
 
-// FP16 and FP8 paths: one accumulation over the whole FFT block (its TMEM rounding
+// FP16 and FP8 paths: one accumulation over each segment of the FFT block (its TMEM rounding
 // bias, ~1e-5 over 2048 FFTs, is far below the FP16 / FP8 quantisation error).
 // A 128-byte SW128 row holds 64 FFTs of FP16 or 128 FFTs of FP8 (E4M3) values;
 // either way one MMA consumes 32 bytes of every row (K = 16 or 32).
+//
+// Work is a list of segments per CTA, each a run of K chunks [k0, k1) (KC FFTs each) of one
+// channel group g: the block's TMEM accumulation of that run, then its epilogue.  A segment that
+// starts at chunk 0 adds into accumulator plane 0, one that starts later into plane 1;
+// finalisation adds the planes.
+//   persist = 0: grid = groups x kparts; CTA b covers group b mod groups, the chunks of its part.
+//   persist = 1: grid = the SM count G, groups >= G.  CTA b takes whole groups b, b + G, ... for
+//     the full rounds, so the CTAs running together work on neighbouring groups (two groups share
+//     every 64-byte row of a 16-channel tile, read from DRAM once); the groups of the last,
+//     partial round are halved in K and shared by pairs of CTAs when they are at most half the
+//     CTAs, so fewer SMs wait out a last partial wave.  Each group is split at most once.
+// Returns false past the CTA's last segment (an empty half is skipped, not returned).
+__device__ __forceinline__ bool xstage_seg(const Params &p, int nck, int KC, int i, int *g, int *k0, int *k1) {
+  if (!p.persist) {
+    if (i > 0) return false;
+    const int kpart = (int)blockIdx.x / p.ngrp;
+    const int kck = (p.kspan + KC - 1) / KC;  // chunks of one part (kspan = nt when unsplit)
+    *g = (int)blockIdx.x - kpart * p.ngrp;
+    *k0 = kpart * kck;
+    *k1 = *k0 + kck < nck ? *k0 + kck : nck;
+    return *k1 > *k0;
+  }
+  const int G = (int)gridDim.x, b = (int)blockIdx.x;
+  const int rounds = p.ngrp / G, rem = p.ngrp - rounds * G;
+  if (i < rounds) {
+    *g = i * G + b;
+    *k0 = 0;
+    *k1 = nck;
+    return true;
+  }
+  if (i > rounds) return false;
+  if (2 * rem > G) {  // too many leftover groups to halve: whole groups, one per CTA
+    if (b >= rem) return false;
+    *g = rounds * G + b;
+    *k0 = 0;
+    *k1 = nck;
+    return true;
+  }
+  if (b >= 2 * rem) return false;
+  const int kh = (nck + 1) / 2;
+  *g = rounds * G + b / 2;
+  *k0 = (b & 1) ? kh : 0;
+  *k1 = (b & 1) ? nck : kh;
+  return *k1 > *k0;
+}
+
 template <bool F8>
 __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, const __grid_constant__ CUtensorMap tmap) {
   using C = Cfg<false>;
@@ -117,22 +166,15 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
   constexpr int TMEM_COLS = C::TMEM_COLS;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], raw_full[RSTAGES], raw_empty[RSTAGES],
-      bar_done;
+      bar_done, bar_tfree, bar_final;
   __shared__ uint32_t tmem_base_sh;
   // 128-byte swizzle atoms need 1024-byte alignment of the shared-window address
   unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   const uint32_t sbase = smem_u32(smem);
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
-  const int ngrp = (int)gridDim.x / p.kparts;
-  const int kpart = (int)blockIdx.x / ngrp;
-  const int cb = ((int)blockIdx.x - kpart * ngrp) * p.CS;  // first channel of this CTA
   const int n = p.nstream;
-  const int kt0 = kpart * p.kspan;  // first FFT of this CTA's share of the block
-  const int ntl = p.nt - kt0 < p.kspan ? p.nt - kt0 : p.kspan;
-  const int nchunks = (ntl + KC - 1) / KC;
-  float2 *const vsum = p.vsum + (size_t)kpart * p.plane;
-  float2 *const vcomp = p.vcomp + (size_t)kpart * p.plane;
+  const int nck = (p.nt + KC - 1) / KC;  // K chunks of a group
 
   // zero the padding rows (2n..R-1 of each channel block) of the ring once; producers never write them
   if (2 * n < p.R) {
@@ -157,6 +199,8 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
       mbar_init(smem_u32(&raw_empty[s]), NPROD_WARPS);
     }
     mbar_init(smem_u32(&bar_done), 1);
+    mbar_init(smem_u32(&bar_tfree), 4);  // the four epilogue warps have read a segment's TMEM
+    mbar_init(smem_u32(&bar_final), 1);
     fence_mbar_init();
   }
   if (warp == NPROD_WARPS) {
@@ -173,218 +217,258 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
   constexpr int ESZ = F8 ? 2 : 4;             // bytes per complex value
   const int KCR = p.rkc;                      // FFTs per raw chunk (divides KC)
   const int RPO = KC / KCR;                   // raw chunks per operand stage
-  const int nraw = nchunks * RPO;
   if (warp == TMA_WARP) {
     // ------------------------------------------------------------ TMA producer
-    // One lane streams the block through the raw ring: one box per channel tile,
+    // One lane streams every segment's chunks through the raw ring: one box per channel tile,
     // [t][stream][rbx channels] as stored, rows past the block's FFT count zero-filled.
     if (lane == 0) {
-      const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(p.rbx - 1)) : 0;
       const uint32_t raw_s = sbase + STAGES * STAGE_BYTES;
-      int issued = 0;
-      for (int rc = 0; rc < nraw; rc++) {
-        const int rs = rc % RSTAGES;
-        if (rc >= RSTAGES && !mbar_wait(smem_u32(&raw_empty[rs]), ((rc / RSTAGES) - 1) & 1, p.err)) break;
-        const uint32_t bar = smem_u32(&raw_full[rs]);
-        mbar_expect_tx(bar, (uint32_t)(p.rbox_bytes * p.rnbox));
-        for (int j = 0; j < p.rnbox; j++)
-          tma_load_4d(raw_s + rs * RAW_BYTES + j * p.rbox_bytes, &tmap, x0, 0, kt0 + rc * KCR, (cb >> 4) + j, bar);
-        issued = rc + 1;
+      int rc = 0;  // raw chunks issued by this CTA
+      bool ok = true;
+      int g, k0, k1;
+      for (int i = 0; ok && xstage_seg(p, nck, KC, i, &g, &k0, &k1); i++) {
+        const int cb = g * p.CS;
+        const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(p.rbx - 1)) : 0;
+        for (int k = k0; k < k1 && ok; k++)
+          for (int r = 0; r < RPO; r++, rc++) {
+            const int rs = rc % RSTAGES;
+            if (rc >= RSTAGES && !mbar_wait(smem_u32(&raw_empty[rs]), ((rc / RSTAGES) - 1) & 1, p.err)) {
+              ok = false;
+              break;
+            }
+            const uint32_t bar = smem_u32(&raw_full[rs]);
+            mbar_expect_tx(bar, (uint32_t)(p.rbox_bytes * p.rnbox));
+            for (int j = 0; j < p.rnbox; j++)
+              tma_load_4d(raw_s + rs * RAW_BYTES + j * p.rbox_bytes, &tmap, x0, 0, k * KC + r * KCR, (cb >> 4) + j,
+                          bar);
+          }
       }
       // every copy issued lands before the CTA can exit (the last RSTAGES are the only
       // ones possibly unconsumed, and no later phase of their stages was started)
-      for (int rc = issued > RSTAGES ? issued - RSTAGES : 0; rc < issued; rc++)
-        mbar_wait_drain(smem_u32(&raw_full[rc % RSTAGES]), (rc / RSTAGES) & 1);
+      for (int c = rc > RSTAGES ? rc - RSTAGES : 0; c < rc; c++)
+        mbar_wait_drain(smem_u32(&raw_full[c % RSTAGES]), (c / RSTAGES) & 1);
     }
   } else if (warp < NPROD_WARPS) {
-    // ------------------------------------------------------------ producers
+    // ------------------------------------------------------------ producers (+ epilogue: warps 0-3)
     // Corner-turn each raw chunk into K-contiguous SW128 rows of the operand stage;
-    // every warp releases the raw stage on its own (raw_empty counts warps).
+    // every warp releases the raw stage on its own (raw_empty counts warps).  After a
+    // segment's last chunk warps 0-3 fold its TMEM sums into the accumulators.
     const int BX = p.rbx, boxb = p.rbox_bytes;
-    const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(BX - 1)) : 0;
-    const int cofs = p.rnbox == 1 ? (cb & 15) - x0 : 0;  // box index of this CTA's first channel
     const unsigned char *raw0 = smem + STAGES * STAGE_BYTES;
     const int nq = p.CS / 4;                  // channel quads (CS >= 4)
     const int kq = KCR / TK;                  // K chunks per raw chunk
     const int ntask = kq * n * nq;            // (channel quad, stream, K chunk) per raw chunk
     const size_t tstride = (size_t)n * BX * ESZ;  // bytes between FFT rows of a box
     bool ok = true;
-    for (int ch = 0; ch < nchunks && ok; ch++) {
-      const int st = ch % STAGES;
-      if (ch >= STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err)) break;
-      unsigned char *stage = smem + (size_t)st * STAGE_BYTES;
-      for (int r = 0; r < RPO; r++) {
-        const int rc = ch * RPO + r;
-        const int rs = rc % RSTAGES;
-        if (!mbar_wait(smem_u32(&raw_full[rs]), (rc / RSTAGES) & 1, p.err)) {
+    int ch = 0;  // operand chunks produced by this CTA
+    int sg = 0;  // segments finished
+    int g, k0, k1;
+    for (int i = 0; ok && xstage_seg(p, nck, KC, i, &g, &k0, &k1); i++) {
+      const int cb = g * p.CS;  // first channel of the segment
+      const int x0 = p.rnbox == 1 ? ((cb & 15) & ~(BX - 1)) : 0;
+      const int cofs = p.rnbox == 1 ? (cb & 15) - x0 : 0;  // box index of the segment's first channel
+      for (int k = k0; k < k1 && ok; k++, ch++) {
+        const int st = ch % STAGES;
+        if (ch >= STAGES && !mbar_wait(smem_u32(&bar_empty[st]), ((ch / STAGES) - 1) & 1, p.err)) {
           ok = false;
           break;
         }
-        const unsigned char *raw = raw0 + rs * RAW_BYTES;
-        // task = (channel quad q, stream s, K chunk o), q then s fastest across lanes:
-        // a warp reads consecutive 16-byte (or 8-byte) pieces of one FFT row
-        for (int task0 = tid; task0 < ntask; task0 += 2 * NPROD) {
-#pragma unroll
-          for (int u2 = 0; u2 < 2; u2++) {
-            const int task = task0 + u2 * NPROD;
-            if (task >= ntask) break;
-            const int q = task % nq;
-            const int rest = task / nq;
-            const int s = rest % n;
-            const int o = rest / n;
-            const int oo = r * kq + o;      // K chunk within the 128-byte row
-            const int cc0 = cofs + 4 * q;   // first channel of the quad, counted in the boxes
-            // which of the pair (re row, im row) this lane stores first: among 8 lanes the
-            // first stores then cover all 8 swizzle positions (no bank conflicts)
-            const int sw = nq == 1 ? ((s >> 2) & 1) : (q & 1);
-            const unsigned char *src =
-                raw + (cc0 >> 4) * boxb + ((size_t)(o * TK) * n + s) * BX * ESZ + (cc0 & 15) * ESZ;
-            if constexpr (F8) {
-              // 16 FFTs x 4 channels of E4M3 pairs (8 bytes per FFT) -> 8 rows (4 channels x re/im)
-              // of 16 FFT bytes: two prmt gather one channel's (re, im) bytes of 2 FFTs each, a
-              // third and fourth split them into 4 re bytes and 4 im bytes
-              uint2 v[16];
-#pragma unroll
-              for (int i = 0; i < 16; i++) v[i] = *reinterpret_cast<const uint2 *>(src + i * tstride);
-#pragma unroll
-              for (int ci = 0; ci < 4; ci++) {
-                const int cc = 4 * q + ci;
-                const int G = cc / p.g, gi = cc - G * p.g;
-                const int row = gi * p.R + 2 * s;
-                const uint32_t sel = (ci & 1) ? 0x7362u : 0x5140u;
-                uint32_t re[4], im[4];
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                  const uint32_t a0 = (ci < 2) ? v[4 * k].x : v[4 * k].y;
-                  const uint32_t a1 = (ci < 2) ? v[4 * k + 1].x : v[4 * k + 1].y;
-                  const uint32_t a2 = (ci < 2) ? v[4 * k + 2].x : v[4 * k + 2].y;
-                  const uint32_t a3 = (ci < 2) ? v[4 * k + 3].x : v[4 * k + 3].y;
-                  const uint32_t t0 = prmt(a0, a1, sel), t1 = prmt(a2, a3, sel);
-                  re[k] = prmt(t0, t1, 0x5410);
-                  im[k] = prmt(t0, t1, 0x7632);
+        unsigned char *stage = smem + (size_t)st * STAGE_BYTES;
+        for (int r = 0; r < RPO; r++) {
+          const int rc = ch * RPO + r;
+          const int rs = rc % RSTAGES;
+          if (!mbar_wait(smem_u32(&raw_full[rs]), (rc / RSTAGES) & 1, p.err)) {
+            ok = false;
+            break;
+          }
+          const unsigned char *raw = raw0 + rs * RAW_BYTES;
+            // task = (channel quad q, stream s, K chunk o), q then s fastest across lanes:
+            // a warp reads consecutive 16-byte (or 8-byte) pieces of one FFT row
+            for (int task0 = tid; task0 < ntask; task0 += 2 * NPROD) {
+    #pragma unroll
+              for (int u2 = 0; u2 < 2; u2++) {
+                const int task = task0 + u2 * NPROD;
+                if (task >= ntask) break;
+                const int q = task % nq;
+                const int rest = task / nq;
+                const int s = rest % n;
+                const int o = rest / n;
+                const int oo = r * kq + o;      // K chunk within the 128-byte row
+                const int cc0 = cofs + 4 * q;   // first channel of the quad, counted in the boxes
+                // which of the pair (re row, im row) this lane stores first: among 8 lanes the
+                // first stores then cover all 8 swizzle positions (no bank conflicts)
+                const int sw = nq == 1 ? ((s >> 2) & 1) : (q & 1);
+                const unsigned char *src =
+                    raw + (cc0 >> 4) * boxb + ((size_t)(o * TK) * n + s) * BX * ESZ + (cc0 & 15) * ESZ;
+                if constexpr (F8) {
+                  // 16 FFTs x 4 channels of E4M3 pairs (8 bytes per FFT) -> 8 rows (4 channels x re/im)
+                  // of 16 FFT bytes: two prmt gather one channel's (re, im) bytes of 2 FFTs each, a
+                  // third and fourth split them into 4 re bytes and 4 im bytes
+                  uint2 v[16];
+    #pragma unroll
+                  for (int i = 0; i < 16; i++) v[i] = *reinterpret_cast<const uint2 *>(src + i * tstride);
+    #pragma unroll
+                  for (int ci = 0; ci < 4; ci++) {
+                    const int cc = 4 * q + ci;
+                    const int G = cc / p.g, gi = cc - G * p.g;
+                    const int row = gi * p.R + 2 * s;
+                    const uint32_t sel = (ci & 1) ? 0x7362u : 0x5140u;
+                    uint32_t re[4], im[4];
+    #pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                      const uint32_t a0 = (ci < 2) ? v[4 * k].x : v[4 * k].y;
+                      const uint32_t a1 = (ci < 2) ? v[4 * k + 1].x : v[4 * k + 1].y;
+                      const uint32_t a2 = (ci < 2) ? v[4 * k + 2].x : v[4 * k + 2].y;
+                      const uint32_t a3 = (ci < 2) ? v[4 * k + 3].x : v[4 * k + 3].y;
+                      const uint32_t t0 = prmt(a0, a1, sel), t1 = prmt(a2, a3, sel);
+                      re[k] = prmt(t0, t1, 0x5410);
+                      im[k] = prmt(t0, t1, 0x7632);
+                    }
+                    const uint4 vre = make_uint4(re[0], re[1], re[2], re[3]);
+                    const uint4 vim = make_uint4(im[0], im[1], im[2], im[3]);
+                    const int ra = row + sw, rb = row + 1 - sw;
+                    unsigned char *gbase = stage + G * GROUP_BYTES;
+                    *reinterpret_cast<uint4 *>(gbase + ra * 128 + ((oo ^ (ra & 7)) << 4)) = sw ? vim : vre;
+                    *reinterpret_cast<uint4 *>(gbase + rb * 128 + ((oo ^ (rb & 7)) << 4)) = sw ? vre : vim;
+                  }
+                } else {
+                  // 8 FFTs x 4 channels of FP16 complex -> 8 rows (4 channels x re/im) of 8 FFTs
+                  uint4 v[8];
+    #pragma unroll
+                  for (int i = 0; i < 8; i++) v[i] = *reinterpret_cast<const uint4 *>(src + i * tstride);
+    #pragma unroll
+                  for (int ci = 0; ci < 4; ci++) {
+                    const int cc = 4 * q + ci;
+                    const int G = cc / p.g, gi = cc - G * p.g;
+                    const int row = gi * p.R + 2 * s;
+                    uint32_t w[8];
+    #pragma unroll
+                    for (int i = 0; i < 8; i++)
+                      w[i] = (ci == 0) ? v[i].x : (ci == 1) ? v[i].y : (ci == 2) ? v[i].z : v[i].w;
+                    const uint4 vre = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410),
+                                                 prmt(w[4], w[5], 0x5410), prmt(w[6], w[7], 0x5410));
+                    const uint4 vim = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632),
+                                                 prmt(w[4], w[5], 0x7632), prmt(w[6], w[7], 0x7632));
+                    const int ra = row + sw, rb = row + 1 - sw;
+                    unsigned char *gbase = stage + G * GROUP_BYTES;
+                    *reinterpret_cast<uint4 *>(gbase + ra * 128 + ((oo ^ (ra & 7)) << 4)) = sw ? vim : vre;
+                    *reinterpret_cast<uint4 *>(gbase + rb * 128 + ((oo ^ (rb & 7)) << 4)) = sw ? vre : vim;
+                  }
                 }
-                const uint4 vre = make_uint4(re[0], re[1], re[2], re[3]);
-                const uint4 vim = make_uint4(im[0], im[1], im[2], im[3]);
-                const int ra = row + sw, rb = row + 1 - sw;
-                unsigned char *gbase = stage + G * GROUP_BYTES;
-                *reinterpret_cast<uint4 *>(gbase + ra * 128 + ((oo ^ (ra & 7)) << 4)) = sw ? vim : vre;
-                *reinterpret_cast<uint4 *>(gbase + rb * 128 + ((oo ^ (rb & 7)) << 4)) = sw ? vre : vim;
               }
-            } else {
-              // 8 FFTs x 4 channels of FP16 complex -> 8 rows (4 channels x re/im) of 8 FFTs
-              uint4 v[8];
+            }
+          __syncwarp();  // this warp's reads of the raw stage are done (their values are stored)
+          if (lane == 0) mbar_arrive(smem_u32(&raw_empty[rs]));
+        }
+        if (!ok) break;
+        fence_proxy_async_smem();
+        mbar_arrive(smem_u32(&bar_full[st]));
+      }
+      if (!ok) break;
+      // ------------------------------------------------------------ epilogue of the segment
+      if (warp < 4) {
+        ok = mbar_wait(smem_u32(&bar_done), sg & 1, p.err);
+        tc_fence_after();
+        if (ok) {
+          float2 *const vsum = p.vsum + (k0 > 0 ? p.plane : 0);
+          float2 *const vcomp = p.vcomp + (k0 > 0 ? p.plane : 0);
+          const int row = 32 * warp + lane;
+          const int my_gi = row / p.R;
+          const int r = row - my_gi * p.R;
+          const int s1 = r >> 1, part1 = r & 1;
+          const int gi0 = (32 * warp) / p.R;
+          const int col0 = gi0 * p.R;
+          const int clen = p.R > 32 ? p.R : 32;
+          const int j = s1 >> 1, l = s1 & 1;
+          for (int G = 0; G < NG; G++) {
+            const int c = cb + G * p.g + my_gi;
+            // up to two 16-column pieces (8 outputs) per accumulator batch
+            for (int pc0 = 0; pc0 < clen; pc0 += 32) {
+              size_t off[8];
+              float2 val[8];
+              bool use[8];
 #pragma unroll
-              for (int i = 0; i < 8; i++) v[i] = *reinterpret_cast<const uint4 *>(src + i * tstride);
+              for (int uu = 0; uu < 2; uu++) {
 #pragma unroll
-              for (int ci = 0; ci < 4; ci++) {
-                const int cc = 4 * q + ci;
-                const int G = cc / p.g, gi = cc - G * p.g;
-                const int row = gi * p.R + 2 * s;
-                uint32_t w[8];
+                for (int qq = 0; qq < 4; qq++) use[4 * uu + qq] = false;
+                const int pc = pc0 + 16 * uu;
+                if (pc >= clen) continue;  // the same for the whole warp
+                __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skip below
+                const int col = col0 + pc;
+                float v[16], pv[16];
+                tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(G * 128 + col), v);
 #pragma unroll
-                for (int i = 0; i < 8; i++)
-                  w[i] = (ci == 0) ? v[i].x : (ci == 1) ? v[i].y : (ci == 2) ? v[i].z : v[i].w;
-                const uint4 vre = make_uint4(prmt(w[0], w[1], 0x5410), prmt(w[2], w[3], 0x5410),
-                                             prmt(w[4], w[5], 0x5410), prmt(w[6], w[7], 0x5410));
-                const uint4 vim = make_uint4(prmt(w[0], w[1], 0x7632), prmt(w[2], w[3], 0x7632),
-                                             prmt(w[4], w[5], 0x7632), prmt(w[6], w[7], 0x7632));
-                const int ra = row + sw, rb = row + 1 - sw;
-                unsigned char *gbase = stage + G * GROUP_BYTES;
-                *reinterpret_cast<uint4 *>(gbase + ra * 128 + ((oo ^ (ra & 7)) << 4)) = sw ? vim : vre;
-                *reinterpret_cast<uint4 *>(gbase + rb * 128 + ((oo ^ (rb & 7)) << 4)) = sw ? vre : vim;
+                for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
+                if (col < my_gi * p.R || col >= (my_gi + 1) * p.R || s1 >= n) continue;
+                const int s2b = (col - my_gi * p.R) >> 1;
+#pragma unroll
+                for (int qq = 0; qq < 4; qq++) {
+                  const int q = qq + 4 * part1;
+                  const int s2 = s2b + q;
+                  if (s2 >= n) continue;
+                  const int k = s2 >> 1, m = s2 & 1;
+                  if (j > k || (j == k && !p.autos)) continue;
+                  float re, im;
+                  if (part1 == 0) {
+                    re = v[2 * q] + pv[2 * q + 1];
+                    im = pv[2 * q] - v[2 * q + 1];
+                  } else {
+                    re = pv[2 * q] + v[2 * q + 1];
+                    im = v[2 * q] - pv[2 * q + 1];
+                  }
+                  const int bl = baseline_index(j, k, p.nant);
+                  use[4 * uu + qq] = true;
+                  val[4 * uu + qq] = make_float2(re, im);
+                  off[4 * uu + qq] = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
+                }
               }
+              rmw_batch<8>(vsum, vcomp, off, val, use);
             }
           }
         }
-        __syncwarp();  // this warp's reads of the raw stage are done (their values are stored)
-        if (lane == 0) mbar_arrive(smem_u32(&raw_empty[rs]));
+        // this warp's TMEM reads of the segment are done: the MMAs of the next segment may
+        // overwrite the accumulators
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&bar_tfree));
       }
-      if (!ok) break;
-      fence_proxy_async_smem();
-      mbar_arrive(smem_u32(&bar_full[st]));
+      sg++;
     }
   } else if (lane == 0) {
     // ------------------------------------------------------------ MMA issuer
-    for (int ch = 0; ch < nchunks; ch++) {
-      const int st = ch % STAGES;
-      if (!mbar_wait(smem_u32(&bar_full[st]), (ch / STAGES) & 1, p.err)) break;
+    int ch = 0, sg = 0;
+    bool ok = true;
+    int g, k0, k1;
+    for (int i = 0; ok && xstage_seg(p, nck, KC, i, &g, &k0, &k1); i++) {
+      // the previous segment's epilogue has read the accumulators this one starts afresh
+      if (sg > 0 && !mbar_wait(smem_u32(&bar_tfree), (sg - 1) & 1, p.err)) break;
       tc_fence_after();
-      const uint32_t sa = sbase + st * STAGE_BYTES;
-#pragma unroll
-      for (int G = 0; G < NG; G++) {
-#pragma unroll
-        for (int kk = 0; kk < KC / KSTEP; kk++) {
-          const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
-          const uint64_t dh = desc_sw128(sa + G * GROUP_BYTES + kk * 32);
-          if constexpr (F8) mma_f8(tmem + G * 128, dh, dh, IDESC, acc);
-          else mma_f16(tmem + G * 128, dh, dh, IDESC, acc);
+      for (int k = k0; k < k1; k++, ch++) {
+        const int st = ch % STAGES;
+        if (!mbar_wait(smem_u32(&bar_full[st]), (ch / STAGES) & 1, p.err)) {
+          ok = false;
+          break;
         }
-      }
-      mma_commit(smem_u32(&bar_empty[st]));
-    }
-    mma_commit(smem_u32(&bar_done));
-    mbar_wait(smem_u32(&bar_done), 0, p.err);  // issued MMAs drained before TMEM is read or freed
-  }
-
-  // ------------------------------------------------------------ epilogue
-  if (warp < 4) {
-    const bool ok = mbar_wait(smem_u32(&bar_done), 0, p.err);
-    tc_fence_after();
-    if (ok) {
-      const int row = 32 * warp + lane;
-      const int my_gi = row / p.R;
-      const int r = row - my_gi * p.R;
-      const int s1 = r >> 1, part1 = r & 1;
-      const int gi0 = (32 * warp) / p.R;
-      const int col0 = gi0 * p.R;
-      const int clen = p.R > 32 ? p.R : 32;
-      const int j = s1 >> 1, l = s1 & 1;
-      for (int G = 0; G < NG; G++) {
-        const int c = cb + G * p.g + my_gi;
-        // up to two 16-column pieces (8 outputs) per accumulator batch
-        for (int pc0 = 0; pc0 < clen; pc0 += 32) {
-          size_t off[8];
-          float2 val[8];
-          bool use[8];
+        tc_fence_after();
+        const uint32_t sa = sbase + st * STAGE_BYTES;
 #pragma unroll
-          for (int u = 0; u < 2; u++) {
+        for (int G = 0; G < NG; G++) {
 #pragma unroll
-            for (int qq = 0; qq < 4; qq++) use[4 * u + qq] = false;
-            const int pc = pc0 + 16 * u;
-            if (pc >= clen) continue;  // the same for the whole warp
-            __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skip below
-            const int col = col0 + pc;
-            float v[16], pv[16];
-            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(G * 128 + col), v);
-#pragma unroll
-            for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
-            if (col < my_gi * p.R || col >= (my_gi + 1) * p.R || s1 >= n) continue;
-            const int s2b = (col - my_gi * p.R) >> 1;
-#pragma unroll
-            for (int qq = 0; qq < 4; qq++) {
-              const int q = qq + 4 * part1;
-              const int s2 = s2b + q;
-              if (s2 >= n) continue;
-              const int k = s2 >> 1, m = s2 & 1;
-              if (j > k || (j == k && !p.autos)) continue;
-              float re, im;
-              if (part1 == 0) {
-                re = v[2 * q] + pv[2 * q + 1];
-                im = pv[2 * q] - v[2 * q + 1];
-              } else {
-                re = pv[2 * q] + v[2 * q + 1];
-                im = v[2 * q] - pv[2 * q + 1];
-              }
-              const int bl = baseline_index(j, k, p.nant);
-              use[4 * u + qq] = true;
-              val[4 * u + qq] = make_float2(re, im);
-              off[4 * u + qq] = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
-            }
+          for (int kk = 0; kk < KC / KSTEP; kk++) {
+            const uint32_t acc = (k > k0 || kk > 0) ? 1u : 0u;
+            const uint64_t dh = desc_sw128(sa + G * GROUP_BYTES + kk * 32);
+            if constexpr (F8) mma_f8(tmem + G * 128, dh, dh, IDESC, acc);
+            else mma_f16(tmem + G * 128, dh, dh, IDESC, acc);
           }
-          rmw_batch<8>(vsum, vcomp, off, val, use);
         }
+        mma_commit(smem_u32(&bar_empty[st]));
       }
+      if (!ok) break;
+      mma_commit(smem_u32(&bar_done));
+      sg++;
     }
+    mma_commit(smem_u32(&bar_final));
+    mbar_wait(smem_u32(&bar_final), 0, p.err);  // issued MMAs drained before TMEM is freed
   }
   tc_fence_before();
   __syncthreads();
@@ -1280,6 +1364,8 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   p.vsum = vsum;
   p.vcomp = vcomp;
   p.kparts = 1;
+  p.persist = 0;
+  p.ngrp = 0;
   p.kspan = nt;
   p.plane = plane;
   // FP32 data: FP16 hi/lo split of values scaled by 2^-split_e when split_e >= 0, else TF32 split
@@ -1354,14 +1440,20 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
+    p.ngrp = ngrp;
+    p.persist = 0;
     if (kparts_max >= 2 && plane > 0 && nt >= 4 * KC && (ngrp < nsm || kparts_max >= 3)) {
       p.kparts = 2;
       p.kspan = (nt / 2 + KC - 1) / KC * KC;
+    } else if (kparts_max == 2 && plane > 0 && ngrp >= nsm) {
+      // at least as many groups as SMs: one CTA per SM, each an equal share of all (group, K
+      // chunk) units, so no SM idles in a last partial wave (512 groups are 3.37 waves)
+      p.persist = 1;
     }
     auto kern = chan_type == CHAN_F8 ? tc::xstage_tc_kernel<true> : tc::xstage_tc_kernel<false>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    kern<<<ngrp * p.kparts, tc::NTHREADS_TC, smem, s>>>(p, tmap);
+    kern<<<p.persist ? nsm : ngrp * p.kparts, tc::NTHREADS_TC, smem, s>>>(p, tmap);
   }
   return cudaGetLastError();
 }
