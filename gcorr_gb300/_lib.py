@@ -41,6 +41,8 @@ EXPORTS = [
     "gxc_conf_antenna_file", "gxc_conf_delays", "gxc_conf_free", "gxc_reader_open", "gxc_reader_read",
     "gxc_reader_close", "gxc_save_visibilities", "gxc_host_alloc", "gxc_host_free", "gxc_set_frame_validity",
     "gxc_vdif_parse_header", "gxc_vdif_depacketize", "gxc_probe_unpack",
+    "gxc_dada_parse_header", "gxc_dada_header_value", "gxc_dada_config", "gxc_dada_open", "gxc_dada_header_of",
+    "gxc_dada_read", "gxc_dada_close",
 ]
 
 
@@ -56,6 +58,13 @@ class GxcVdifHeader(C.Structure):
                 ("frame", C.c_int), ("version", C.c_int), ("nchan", C.c_int), ("frame_bytes", C.c_int),
                 ("is_complex", C.c_int), ("bits", C.c_int), ("thread", C.c_int), ("station", C.c_int),
                 ("header_bytes", C.c_int)]
+
+
+class GxcDadaHeader(C.Structure):
+    _fields_ = [("hdr_size", C.c_longlong), ("nbit", C.c_int), ("npol", C.c_int), ("ndim", C.c_int),
+                ("nchan", C.c_int), ("bw_mhz", C.c_double), ("freq_mhz", C.c_double), ("tsamp_us", C.c_double),
+                ("bytes_per_second", C.c_longlong), ("obs_offset", C.c_longlong), ("picoseconds", C.c_longlong),
+                ("mjd_start", C.c_double), ("utc_start", C.c_char * 32), ("source", C.c_char * 64)]
 
 
 class GxcJob(C.Structure):
@@ -121,6 +130,20 @@ def lib():
         l.gxc_last_error.restype = C.c_char_p
         l.gxc_last_launch_count.argtypes = [V]
         l.gxc_last_launch_count.restype = C.c_int
+        l.gxc_dada_parse_header.argtypes = [C.c_char_p, C.c_size_t, P(GxcDadaHeader)]
+        l.gxc_dada_parse_header.restype = C.c_int
+        l.gxc_dada_header_value.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p, C.c_char_p, C.c_size_t]
+        l.gxc_dada_header_value.restype = C.c_int
+        l.gxc_dada_config.argtypes = [P(GxcDadaHeader), P(GxcConfig)]
+        l.gxc_dada_config.restype = C.c_int
+        l.gxc_dada_open.argtypes = [V, C.c_int, C.c_size_t, C.c_int, P(V)]
+        l.gxc_dada_open.restype = C.c_int
+        l.gxc_dada_header_of.argtypes = [V, C.c_int, P(GxcDadaHeader)]
+        l.gxc_dada_header_of.restype = C.c_int
+        l.gxc_dada_read.argtypes = [V, V]
+        l.gxc_dada_read.restype = C.c_int
+        l.gxc_dada_close.argtypes = [V]
+        l.gxc_dada_close.restype = C.c_int
         l.gxc_probe_unpack.argtypes = [V, V]
         l.gxc_probe_unpack.restype = C.c_int
         l.gxc_fft_block.argtypes = [V]

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgxcorr.so")
 SOURCES = ["gxc_api.cu", "fstage.cu", "fstage_probe.cu", "fstage_tc.cu", "xstage_fp32.cu", "xstage_tc.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "batch_api.cu",
-           "pipeline_api.cu", "conf_io.cpp", "vdif.cu"]
+           "pipeline_api.cu", "conf_io.cpp", "dada_io.cpp", "vdif.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # command-line drivers with the reference harness's interface, linked against the library
 APPS = ["testfxkernel", "bench_fxkernel"]

@@ -312,6 +312,37 @@ gxc_status gxc_vdif_depacketize(const uint8_t *frames, size_t nbytes, int frame_
                                 int offset_binary_8bit, uint8_t fill, uint8_t *out, size_t nslots, uint8_t *valid,
                                 unsigned long long *stats, void *stream);
 
+/* PSRDADA streams.  The reference's ingest writes each station's VDIF payloads, headers stripped,
+ * into a PSRDADA ring buffer behind an ASCII header ("KEY value  # comment" lines in the first
+ * HDR_SIZE bytes, ingest/src/ingest.c:185-330, ingest/src/dada_header_template_atca.txt).  A
+ * stream saved from such a ring (header, then data) holds one antenna's samples in this engine's
+ * input layout.  gxc_dada_parse_header decodes a header text (absent numbers are -1, absent
+ * reals 0, "unset" strings empty); gxc_dada_header_value returns one key's value token.
+ * gxc_dada_config copies nbit, is_complex (NDIM 2), bw (|BW|) and lo (FREQ - |BW|/2, the band
+ * edge) into cfg and returns GXC_ERR_UNSUPPORTED unless NPOL is 2.  gxc_dada_open opens one stream
+ * per antenna and positions each after its header; every gxc_dada_read then fills bufs[a] with the
+ * next bytes_per_read bytes of stream a (offset_binary_8bit != 0 converts 8-bit offset-binary
+ * samples to two's complement) and returns GXC_END_OF_DATA when any stream ends.  Attaching to a
+ * live shared-memory ring needs the psrdada library and is not built. */
+typedef struct gxc_dada_header {
+  long long hdr_size;                 /* HDR_SIZE (4096 when absent) */
+  int nbit, npol, ndim, nchan;        /* NBIT, NPOL, NDIM (1 real, 2 complex), NCHAN */
+  double bw_mhz, freq_mhz, tsamp_us;  /* BW, FREQ (band centre), TSAMP */
+  long long bytes_per_second, obs_offset, picoseconds;
+  double mjd_start;
+  char utc_start[32];
+  char source[64];
+} gxc_dada_header;
+typedef struct gxc_dada_reader gxc_dada_reader;
+gxc_status gxc_dada_parse_header(const char *text, size_t len, gxc_dada_header *out);
+gxc_status gxc_dada_header_value(const char *text, size_t len, const char *key, char *value, size_t value_len);
+gxc_status gxc_dada_config(const gxc_dada_header *hdr, gxc_config *cfg);
+gxc_status gxc_dada_open(const char *const *paths, int nant, size_t bytes_per_read, int offset_binary_8bit,
+                         gxc_dada_reader **out);
+gxc_status gxc_dada_header_of(const gxc_dada_reader *r, int a, gxc_dada_header *out);
+gxc_status gxc_dada_read(gxc_dada_reader *r, uint8_t *const *bufs);
+gxc_status gxc_dada_close(gxc_dada_reader *r);
+
 /* The X-stage alone, on already-channelised data, as the reference GPU X kernels
  * take it (gcorr/src/gxkernel.h:86-88, CrossCorrAccumHoriz/CCAH2/CCAH3;
  * layout gcorr/src/gxkernel.h:30-44): ants is complex float
