@@ -691,7 +691,7 @@ __global__ void __launch_bounds__(256, 2) fstage_pair_kernel(FParams prm) {
 #pragma unroll
     for (int r = 0; r < R; r++) {
       const float2 x0 = sample(r), x1 = sample(r + R);
-      const float2 w = cmul(wiv, make_float2(kC32[r], -kS32[r]));
+      const float2 w = __ldg(&prm.tw[iv + NB0 * r]);
       const float2 b = cmul(make_float2(x0.x - x1.x, x0.y - x1.y), w);
       u[r].re = make_float2(x0.x + x1.x, b.x);
       u[r].im = make_float2(x0.y + x1.y, b.y);
