@@ -259,6 +259,15 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
     const int kq = KCR / TK;                  // K chunks per raw chunk
     const int ntask = kq * n * nq;            // (channel quad, stream, K chunk) per raw chunk
     const size_t tstride = (size_t)n * BX * ESZ;  // bytes between FFT rows of a box
+    // A thread's tasks are the same in every raw chunk: tid and tid + NPROD (the launcher
+    // keeps ntask <= 2 NPROD).  Decoded once here, packed as q | s << 8 | o << 16, so the
+    // chunk loop does no integer division; g and R are powers of two.
+    auto decode = [&](int task) {
+      const int rest = task / nq, o = rest / n;
+      return (task - rest * nq) | ((rest - o * n) << 8) | (o << 16);
+    };
+    const int tpk0 = decode(tid), tpk1 = decode(tid + NPROD);
+    const int lg = 31 - __clz(p.g), lr = 31 - __clz(p.R);
     bool ok = true;
     int ch = 0;  // operand chunks produced by this CTA
     int sg = 0;  // segments finished
@@ -284,15 +293,13 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
           const unsigned char *raw = raw0 + rs * RAW_BYTES;
             // task = (channel quad q, stream s, K chunk o), q then s fastest across lanes:
             // a warp reads consecutive 16-byte (or 8-byte) pieces of one FFT row
-            for (int task0 = tid; task0 < ntask; task0 += 2 * NPROD) {
-    #pragma unroll
+            {
+    #pragma unroll 1
               for (int u2 = 0; u2 < 2; u2++) {
-                const int task = task0 + u2 * NPROD;
+                const int task = tid + u2 * NPROD;
                 if (task >= ntask) break;
-                const int q = task % nq;
-                const int rest = task / nq;
-                const int s = rest % n;
-                const int o = rest / n;
+                const int pk = u2 ? tpk1 : tpk0;
+                const int q = pk & 255, s = (pk >> 8) & 255, o = pk >> 16;
                 const int oo = r * kq + o;      // K chunk within the 128-byte row
                 const int cc0 = cofs + 4 * q;   // first channel of the quad, counted in the boxes
                 // which of the pair (re row, im row) this lane stores first: among 8 lanes the
@@ -310,8 +317,8 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
     #pragma unroll
                   for (int ci = 0; ci < 4; ci++) {
                     const int cc = 4 * q + ci;
-                    const int G = cc / p.g, gi = cc - G * p.g;
-                    const int row = gi * p.R + 2 * s;
+                    const int G = cc >> lg, gi = cc & (p.g - 1);
+                    const int row = (gi << lr) + 2 * s;
                     const uint32_t sel = (ci & 1) ? 0x7362u : 0x5140u;
                     uint32_t re[4], im[4];
     #pragma unroll
@@ -339,8 +346,8 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
     #pragma unroll
                   for (int ci = 0; ci < 4; ci++) {
                     const int cc = 4 * q + ci;
-                    const int G = cc / p.g, gi = cc - G * p.g;
-                    const int row = gi * p.R + 2 * s;
+                    const int G = cc >> lg, gi = cc & (p.g - 1);
+                    const int row = (gi << lr) + 2 * s;
                     uint32_t w[8];
     #pragma unroll
                     for (int i = 0; i < 8; i++)
@@ -595,6 +602,17 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
     const int ntask = kq * n * nq;     // (pair, stream, K chunk) per raw chunk
     const size_t tstride = (size_t)n * BX * 8;  // bytes between FFT rows of a box
     const float sc = p.split_sc;
+    // A thread's tasks are the same in every raw chunk: tid and tid + NPROD (the launcher
+    // keeps ntask <= 2 NPROD), decoded once here so the chunk loop does no integer division.
+    int tq[2], ts[2], to[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const int task = tid + j * NPROD;
+      const int rest = task / nq;
+      tq[j] = task - rest * nq;
+      to[j] = rest / n;
+      ts[j] = rest - to[j] * n;
+    }
     bool ok = true;
     for (int ch = 0; ch < nchunks && ok; ch++) {
       const int st = ch % STAGES;
@@ -611,15 +629,14 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
         // task = (pair q, stream s, 16-byte K chunk o), q then s fastest across lanes: a warp
         // reads consecutive 16-byte pieces of one FFT row (conflict-free)
         constexpr int UT = H16 ? 1 : 2;  // tasks per thread in flight (TKC float4 loads each)
-        for (int task0 = tid; task0 < ntask; task0 += UT * NPROD) {
+#pragma unroll
+        for (int j0 = 0; j0 < 2; j0 += UT) {
+          if (tid + j0 * NPROD >= ntask) break;
           float4 v[UT][TKC];
 #pragma unroll
           for (int u2 = 0; u2 < UT; u2++) {
-            const int task = task0 + u2 * NPROD;
-            const int q = task % nq;
-            const int rest = task / nq;
-            const int s = rest % n;
-            const int o = rest / n;
+            const int task = tid + (j0 + u2) * NPROD;
+            const int q = tq[j0 + u2], s = ts[j0 + u2], o = to[j0 + u2];
             const int cc0 = cofs + 2 * q;
             const unsigned char *src =
                 raw + (cc0 >> 4) * boxb + ((size_t)(TKC * o) * n + s) * BX * 8 + (cc0 & 15) * 8;
@@ -630,12 +647,9 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
           }
 #pragma unroll
           for (int u2 = 0; u2 < UT; u2++) {
-            const int task = task0 + u2 * NPROD;
+            const int task = tid + (j0 + u2) * NPROD;
             if (task >= ntask) break;
-            const int q = task % nq;
-            const int rest = task / nq;
-            const int s = rest % n;
-            const int o = rest / n;
+            const int q = tq[j0 + u2], s = ts[j0 + u2], o = to[j0 + u2];
             const int oo = rr * kq + o;  // K chunk within the 128-byte row
             // which part (re, im) this lane stores first: among 8 lanes the first stores
             // then cover all 8 swizzle positions (no bank conflicts)
@@ -1402,6 +1416,11 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   while (kc > 8 && (size_t)p.rnbox * p.rbx * p.nstream * kc * esz > (size_t)tc::RAW_BYTES) kc >>= 1;
   p.rkc = kc;
   p.rbox_bytes = p.rbx * p.nstream * kc * esz;
+  // producer tasks per raw chunk, (channel quad or pair, stream, 16-byte K chunk): at most two
+  // per producer thread, which the kernels decode once
+  const int tk = chan_type == CHAN_F32 ? (h16 ? 8 : 4) : chan_type == CHAN_F8 ? 16 : 8;
+  const int per_task = chan_type == CHAN_F32 ? 2 : 4;
+  if ((kc / tk) * p.nstream * (p.CS / per_task) > 2 * tc::NPROD) return cudaErrorInvalidValue;
   if ((size_t)p.rnbox * p.rbox_bytes > (size_t)tc::RAW_BYTES || KC % kc ||
       kc % (chan_type == CHAN_F8 ? 16 : 8))
     return cudaErrorInvalidValue;
