@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
   constexpr int TMEM_COLS = C::TMEM_COLS;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], raw_full[RSTAGES], raw_empty[RSTAGES],
-      bar_done, bar_tfree, bar_final;
+      bar_done, bar_tfree, bar_final, bar_stg[2];
   __shared__ uint32_t tmem_base_sh;
   // 128-byte swizzle atoms need 1024-byte alignment of the shared-window address
   unsigned char *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -176,11 +176,14 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
   const int n = p.nstream;
   const int nck = (p.nt + KC - 1) / KC;  // K chunks of a group
 
-  // zero the padding rows (2n..R-1 of each channel block) of the ring once; producers never write them
-  if (2 * n < p.R) {
+  // zero the padding rows (2n..R-1 of each channel block) of the ring; producers never write
+  // them (done here once, and again after each segment epilogue, which stages its results in
+  // the idle ring)
+  auto zero_padding = [&](int t0, int nthr) {
+    if (2 * n >= p.R) return;
     const int pad = p.R - 2 * n;
     const int per_stage = NG * p.g * pad * 8;  // 16-byte words
-    for (int i = tid; i < STAGES * per_stage; i += NTHREADS_TC) {
+    for (int i = t0; i < STAGES * per_stage; i += nthr) {
       const int st = i / per_stage, r0 = i - st * per_stage;
       const int w = r0 & 7, rr = r0 >> 3;
       const int G = rr / (p.g * pad), rem = rr - G * p.g * pad;
@@ -188,7 +191,8 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
       *reinterpret_cast<uint4 *>(smem + (size_t)st * STAGE_BYTES + G * GROUP_BYTES + row * 128 + w * 16) =
           make_uint4(0, 0, 0, 0);
     }
-  }
+  };
+  zero_padding(tid, NTHREADS_TC);
   if (tid == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(smem_u32(&bar_full[s]), NPROD);
@@ -199,8 +203,10 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
       mbar_init(smem_u32(&raw_empty[s]), NPROD_WARPS);
     }
     mbar_init(smem_u32(&bar_done), 1);
-    mbar_init(smem_u32(&bar_tfree), 4);  // the four epilogue warps have read a segment's TMEM
+    mbar_init(smem_u32(&bar_tfree), NPROD_WARPS);  // every producer warp has read its share of a segment's TMEM
     mbar_init(smem_u32(&bar_final), 1);
+    mbar_init(smem_u32(&bar_stg[0]), NPROD);  // the producers have staged a segment's results
+    mbar_init(smem_u32(&bar_stg[1]), NPROD);  // ... and added them into the accumulators
     fence_mbar_init();
   }
   if (warp == NPROD_WARPS) {
@@ -268,6 +274,9 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
     };
     const int tpk0 = decode(tid), tpk1 = decode(tid + NPROD);
     const int lg = 31 - __clz(p.g), lr = 31 - __clz(p.R);
+    const int lcs = 31 - __clz(p.CS);  // CS is a power of two
+    const int nbl = p.nant * (p.nant - 1) / 2 + (p.autos ? p.nant : 0);
+    const int nent = nbl * 4 * p.CS;   // staged values of a segment (fits the operand ring)
     bool ok = true;
     int ch = 0;  // operand chunks produced by this CTA
     int sg = 0;  // segments finished
@@ -373,63 +382,56 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
       }
       if (!ok) break;
       // ------------------------------------------------------------ epilogue of the segment
-      if (warp < 4) {
+      // The segment's MMAs are done, so the operand ring is idle until the producers start the
+      // next segment: the eight producer warps stage the segment's visibilities there, as
+      // [baseline x product][CS channels], and release tensor memory; then all of them add the
+      // staged values into the accumulators, CS consecutive channels of a (baseline, product)
+      // contiguous in memory, so a warp's loads and stores touch 8 sectors instead of 32.
+      // Warp w reads TMEM lane quarter w % 4 (the lanes a warp may access) of the groups
+      // G = w / 4, w / 4 + 2.  The two producer-wide syncs are mbarriers with bounded waits.
+      {
+        float2 *const stg = reinterpret_cast<float2 *>(smem);
         ok = mbar_wait(smem_u32(&bar_done), sg & 1, p.err);
         tc_fence_after();
         if (ok) {
-          float2 *const vsum = p.vsum + (k0 > 0 ? p.plane : 0);
-          float2 *const vcomp = p.vcomp + (k0 > 0 ? p.plane : 0);
-          const int row = 32 * warp + lane;
+          const int wq = warp & 3;  // TMEM lane quarter
+          const int row = 32 * wq + lane;
           const int my_gi = row / p.R;
           const int r = row - my_gi * p.R;
           const int s1 = r >> 1, part1 = r & 1;
-          const int gi0 = (32 * warp) / p.R;
+          const int gi0 = (32 * wq) / p.R;
           const int col0 = gi0 * p.R;
           const int clen = p.R > 32 ? p.R : 32;
           const int j = s1 >> 1, l = s1 & 1;
-          for (int G = 0; G < NG; G++) {
-            const int c = cb + G * p.g + my_gi;
-            // up to two 16-column pieces (8 outputs) per accumulator batch
-            for (int pc0 = 0; pc0 < clen; pc0 += 32) {
-              size_t off[8];
-              float2 val[8];
-              bool use[8];
+          for (int G = warp >> 2; G < NG; G += 2) {
+            const int cl = G * p.g + my_gi;  // channel within the CTA's CS
+            for (int pc = 0; pc < clen; pc += 16) {
+              __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skip below
+              const int col = col0 + pc;
+              float v[16], pv[16];
+              tmem_ld16(tmem + ((uint32_t)(32 * wq) << 16) + (uint32_t)(G * 128 + col), v);
 #pragma unroll
-              for (int uu = 0; uu < 2; uu++) {
+              for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
+              if (col < my_gi * p.R || col >= (my_gi + 1) * p.R || s1 >= n) continue;
+              const int s2b = (col - my_gi * p.R) >> 1;
 #pragma unroll
-                for (int qq = 0; qq < 4; qq++) use[4 * uu + qq] = false;
-                const int pc = pc0 + 16 * uu;
-                if (pc >= clen) continue;  // the same for the whole warp
-                __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skip below
-                const int col = col0 + pc;
-                float v[16], pv[16];
-                tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(G * 128 + col), v);
-#pragma unroll
-                for (int q = 0; q < 16; q++) pv[q] = __shfl_xor_sync(0xffffffffu, v[q], 1);
-                if (col < my_gi * p.R || col >= (my_gi + 1) * p.R || s1 >= n) continue;
-                const int s2b = (col - my_gi * p.R) >> 1;
-#pragma unroll
-                for (int qq = 0; qq < 4; qq++) {
-                  const int q = qq + 4 * part1;
-                  const int s2 = s2b + q;
-                  if (s2 >= n) continue;
-                  const int k = s2 >> 1, m = s2 & 1;
-                  if (j > k || (j == k && !p.autos)) continue;
-                  float re, im;
-                  if (part1 == 0) {
-                    re = v[2 * q] + pv[2 * q + 1];
-                    im = pv[2 * q] - v[2 * q + 1];
-                  } else {
-                    re = pv[2 * q] + v[2 * q + 1];
-                    im = v[2 * q] - pv[2 * q + 1];
-                  }
-                  const int bl = baseline_index(j, k, p.nant);
-                  use[4 * uu + qq] = true;
-                  val[4 * uu + qq] = make_float2(re, im);
-                  off[4 * uu + qq] = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
+              for (int qq = 0; qq < 4; qq++) {
+                const int q = qq + 4 * part1;
+                const int s2 = s2b + q;
+                if (s2 >= n) continue;
+                const int k = s2 >> 1, m = s2 & 1;
+                if (j > k || (j == k && !p.autos)) continue;
+                float re, im;
+                if (part1 == 0) {
+                  re = v[2 * q] + pv[2 * q + 1];
+                  im = pv[2 * q] - v[2 * q + 1];
+                } else {
+                  re = pv[2 * q] + v[2 * q + 1];
+                  im = v[2 * q] - pv[2 * q + 1];
                 }
+                const int bl = baseline_index(j, k, p.nant);
+                stg[((bl * 4 + 2 * l + m) << lcs) + cl] = make_float2(re, im);
               }
-              rmw_batch<8>(vsum, vcomp, off, val, use);
             }
           }
         }
@@ -438,6 +440,28 @@ __global__ void __launch_bounds__(NTHREADS_TC, 1) xstage_tc_kernel(Params p, con
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_u32(&bar_tfree));
+        mbar_arrive(smem_u32(&bar_stg[0]));
+        ok = ok && mbar_wait(smem_u32(&bar_stg[0]), sg & 1, p.err);
+        if (ok) {
+          float2 *const vsum = p.vsum + (k0 > 0 ? p.plane : 0);
+          float2 *const vcomp = p.vcomp + (k0 > 0 ? p.plane : 0);
+          for (int e0 = tid; e0 < nent; e0 += 8 * NPROD) {
+            size_t off[8];
+            float2 val[8];
+            bool use[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+              const int e = e0 + u * NPROD;
+              use[u] = e < nent;
+              off[u] = (size_t)(e >> lcs) * p.nchan + cb + (e & (p.CS - 1));
+              val[u] = use[u] ? stg[e] : make_float2(0.f, 0.f);
+            }
+            rmw_batch<8>(vsum, vcomp, off, val, use);
+          }
+        }
+        mbar_arrive(smem_u32(&bar_stg[1]));
+        ok = ok && mbar_wait(smem_u32(&bar_stg[1]), sg & 1, p.err);
+        zero_padding(tid, NPROD);  // the staging overwrote them; the next stage's fence covers these writes
       }
       sg++;
     }
@@ -1455,6 +1479,11 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
     // 6 antennas (64 groups) FP16 0.49 -> 0.30 ms; with 512 groups (3.4 waves) the split was
     // slower (9.0 -> 10.3 ms), its halved CTAs paying their pipeline fill and drain twice.
     const int ngrp = nchan / p.CS;
+    // each segment epilogue stages [baseline x product][CS] visibilities in the operand ring
+    const size_t nbl = (size_t)nant * (nant - 1) / 2 + (autos ? nant : 0);
+    if (nbl * 4 * p.CS * sizeof(float2) > (size_t)tc::STAGES * tc::Cfg<false>::STAGE_BYTES ||
+        (p.CS & (p.CS - 1)))
+      return cudaErrorInvalidValue;
     int dev = 0, nsm = 0;
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
