@@ -819,30 +819,27 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
       tc_fence_before();
       mbar_arrive(smem_u32(&bar_drained[b]));
     }
+    // Stage the block's visibilities, [baseline x product][CS channels], in the operand ring (idle
+    // once the last drain is done: every MMA has finished); all threads then add them into the
+    // accumulators below, CS consecutive channels of a (baseline, product) contiguous in memory.
     if (ok && s1 < n) {
       const int j = s1 >> 1, l = s1 & 1;
 #pragma unroll
       for (int G = 0; G < NG; G++) {
-        const int c = cb + G * GCH + my_gi;
+        const int cl = G * GCH + my_gi;  // channel within the CTA's CS
 #pragma unroll
-        for (int a = 0; a < PP; a++) {  // one accumulator batch of 4 outputs per piece
-          size_t off[4];
-          float2 val[4];
-          bool use[4];
+        for (int a = 0; a < PP; a++) {
 #pragma unroll
           for (int qq = 0; qq < 4; qq++) {
-            use[qq] = false;
             const int s2 = 8 * a + qq + 4 * part1;
             if (s2 >= n) continue;
             const int k = s2 >> 1, m = s2 & 1;
             if (j > k || (j == k && !p.autos)) continue;
             const int bl = baseline_index(j, k, p.nant);
-            use[qq] = true;
-            off[qq] = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
             // the Gram sums times split_unsc: exact, a power of two
-            val[qq] = make_float2(acc[G][a][qq].x * p.split_unsc, acc[G][a][qq].y * p.split_unsc);
+            reinterpret_cast<float2 *>(smem)[(bl * 4 + 2 * l + m) * p.CS + cl] =
+                make_float2(acc[G][a][qq].x * p.split_unsc, acc[G][a][qq].y * p.split_unsc);
           }
-          rmw_batch<4>(p.vsum, p.vcomp, off, val, use);
         }
       }
     }
@@ -850,6 +847,25 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  if (!*(volatile int *)p.err) {  // a timed-out role may have left the staging incomplete
+    const int nbl = p.nant * (p.nant - 1) / 2 + (p.autos ? p.nant : 0);
+    const int nent = nbl * 4 * p.CS;
+    const int lcs = 31 - __clz(p.CS);  // CS is a power of two
+    const float2 *stg = reinterpret_cast<const float2 *>(smem);
+    for (int e0 = tid; e0 < nent; e0 += 8 * NTHREADS_SPLIT) {
+      size_t off[8];
+      float2 val[8];
+      bool use[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int e = e0 + u * NTHREADS_SPLIT;
+        use[u] = e < nent;
+        off[u] = (size_t)(e >> lcs) * p.nchan + cb + (e & (p.CS - 1));
+        val[u] = use[u] ? stg[e] : make_float2(0.f, 0.f);
+      }
+      rmw_batch<8>(p.vsum, p.vcomp, off, val, use);
+    }
+  }
   if (warp == NPROD_WARPS) tmem_dealloc(tmem, TMEM_COLS);
 }
 
@@ -1454,6 +1470,10 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   const size_t smem = (size_t)tc::STAGES * 65536 + (size_t)tc::RSTAGES * tc::RAW_BYTES + 1024;
   static_assert(tc::Cfg<true>::STAGE_BYTES == 65536 && tc::Cfg<false>::STAGE_BYTES == 65536, "stage size");
   if (chan_type == CHAN_F32) {
+    // the block's visibilities are staged as [baseline x product][CS] in the operand ring
+    const size_t nbl = (size_t)nant * (nant - 1) / 2 + (autos ? nant : 0);
+    if (nbl * 4 * p.CS * sizeof(float2) > (size_t)tc::STAGES * tc::Cfg<true>::STAGE_BYTES || (p.CS & (p.CS - 1)))
+      return cudaErrorInvalidValue;
     auto launch = [&](auto kern) -> cudaError_t {
       cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e2 != cudaSuccess) return e2;
