@@ -192,6 +192,12 @@ class FxKernel:
     def fft_block(self) -> int:
         return int(L.lib().gxc_fft_block(self._h))
 
+    @property
+    def num_blocks(self) -> int:
+        """F/X passes of the last process() (one more than nfft / fft_block when host inputs start
+        with a short block)."""
+        return int(L.lib().gxc_num_blocks(self._h))
+
     def enable_stage_timing(self, on: bool = True):
         L.check(L.lib().gxc_enable_stage_timing(self._h, int(on)), self._h, "stage timing")
 

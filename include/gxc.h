@@ -175,6 +175,10 @@ gxc_status gxc_probe_unpack(gxc_handle *h, float *decoded);
 int gxc_last_launch_count(const gxc_handle *h);
 /* Effective FFT block (FFTs per F/X pass) chosen for this handle. */
 int gxc_fft_block(const gxc_handle *h);
+/* F/X passes of the last process(): nfft / fft_block rounded up; when the inputs are on the
+   host and the block was chosen, the passes cover 4096, 8192, ... FFTs up to the block (the
+   compute starts after a shorter copy), which can add passes. */
+int gxc_num_blocks(const gxc_handle *h);
 
 /* Stage timing: when enabled, process() records CUDA events around the F-stage
  * and X-stage launches; gxc_stage_times returns the summed milliseconds of the
