@@ -693,11 +693,13 @@ __global__ void __launch_bounds__(NTHREADS_SPLIT, 1) xstage_tc_split_kernel(Para
                     const float4 &f0 = v[u2][2 * i], &f1 = v[u2][2 * i + 1];
                     const float x0v = sc * (ci ? (part ? f0.w : f0.z) : (part ? f0.y : f0.x));
                     const float x1v = sc * (ci ? (part ? f1.w : f1.z) : (part ? f1.y : f1.x));
-                    const __half h0 = __float2half_rn(x0v), h1 = __float2half_rn(x1v);
-                    const __half l0 = __float2half_rn(x0v - __half2float(h0));
-                    const __half l1 = __float2half_rn(x1v - __half2float(h1));
-                    hi[i] = (uint32_t)__half_as_ushort(h0) | ((uint32_t)__half_as_ushort(h1) << 16);
-                    lo[i] = (uint32_t)__half_as_ushort(l0) | ((uint32_t)__half_as_ushort(l1) << 16);
+                    // packed conversions (cvt.rn.f16x2.f32): the same round-to-nearest halves,
+                    // two values and their packing per instruction
+                    const __half2 h = __floats2half2_rn(x0v, x1v);
+                    const float2 hb = __half22float2(h);
+                    const __half2 lw = __floats2half2_rn(x0v - hb.x, x1v - hb.y);
+                    hi[i] = reinterpret_cast<const uint32_t &>(h);
+                    lo[i] = reinterpret_cast<const uint32_t &>(lw);
                   }
                 } else {
 #pragma unroll
