@@ -624,6 +624,7 @@ def main():
     fx.enable_stage_timing(False)
     fft_block = fx.fft_block
     nlaunch = fx.num_blocks  # F (and X) launches of one step
+    f_engine = fx.fft_engine_used
     vis0 = fx.visibilities()
 
     # X-stage comparison (untimed): the same sub-integration through each X engine
@@ -759,7 +760,7 @@ def main():
         return None if not t else t["per_fft"] * ffts_per_launch + t.get("per_launch_const", 0)
 
     # the F-stage kernel this FFT length and precision runs
-    tc_f = (w.fft_len == 8192 and not w.is_complex and args.precision != "fp32" and args.fft_engine == "tensor")
+    tc_f = f_engine == "tensor"  # the F-stage kernel the handle ran
     if tc_f:
         fkern = "fstage_tc_kernel"
     elif w.fft_len == 8192:
@@ -808,7 +809,7 @@ def main():
             "data": "synthetic",
             "config": {"workload": CONFIGS[args.config][0], "nant": w.nant, "nchan": w.nchan, "nfft": w.nfft,
                        "fft_len": w.fft_len, "nbit": w.nbit, "precision": args.precision,
-                       "x_engine": args.x_engine, "fft_engine": args.fft_engine, "fft_block": fx.fft_block,
+                       "x_engine": args.x_engine, "fft_engine": args.fft_engine, "fft_engine_used": f_engine, "fft_block": fx.fft_block,
                        "autos": True,
                        "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 ({in_bytes / 1e9:.1f} GB packed, "

@@ -32,7 +32,7 @@ EXPORTS = [
     "gxc_num_baselines",
     "gxc_status_string", "gxc_create", "gxc_destroy", "gxc_set_input", "gxc_set_delays", "gxc_process",
     "gxc_sync", "gxc_accumulate", "gxc_get_visibilities", "gxc_device_visibilities", "gxc_get_baseline_counts",
-    "gxc_get_valid_flags", "gxc_last_error", "gxc_last_launch_count", "gxc_fft_block", "gxc_num_blocks", "gxc_enable_stage_timing",
+    "gxc_get_valid_flags", "gxc_last_error", "gxc_last_launch_count", "gxc_fft_block", "gxc_num_blocks", "gxc_fft_engine", "gxc_enable_stage_timing",
     "gxc_stage_times", "gxc_xcorr", "gxc_xcorr_noalloc", "gxc_batch_create", "gxc_batch_launch", "gxc_batch_size",
     "gxc_batch_job", "gxc_batch_launch_count", "gxc_batch_destroy", "gxc_pipeline_create", "gxc_pipeline_submit",
     "gxc_pipeline_wait", "gxc_pipeline_sync", "gxc_pipeline_integration", "gxc_pipeline_set_lin2circ",
@@ -150,6 +150,8 @@ def lib():
         l.gxc_fft_block.restype = C.c_int
         l.gxc_num_blocks.argtypes = [V]
         l.gxc_num_blocks.restype = C.c_int
+        l.gxc_fft_engine.argtypes = [V]
+        l.gxc_fft_engine.restype = C.c_int
         l.gxc_enable_stage_timing.argtypes = [V, C.c_int]
         l.gxc_enable_stage_timing.restype = C.c_int
         l.gxc_stage_times.argtypes = [V, V, V, V]

@@ -5,16 +5,20 @@
 // k = k1 + 64 k2 (fxkernel's dofft, fxkernel/src/fxkernel.cpp:569-580, is the
 // plain unnormalised forward DFT this restates):
 //   X[k1 + 64 k2] = sum_n2 W128^(n2 k2) [ W8192^(n2 k1) sum_n1 W64^(n1 k1) x[n2 + 128 n1] ].
-// Step 1 is a real GEMM per polarisation, D1 (128 x 128) = A1 (128 x 128) B1^T,
+// Step 1 is a real GEMM per polarisation, D1 (128 x 128) = B1 (128 x 128) A1^T,
 // with A1 the real form of DFT64 (row 2 k1 gives Re Y, row 2 k1 + 1 gives Im Y;
 // K = [Re x over n1 | Im x over n1]) and B1 the decoded, fringe-rotated window
-// (row n2, K as for A1).  The twiddle W8192^(n2 k1) is applied on the CUDA cores
+// (row n2, K as for A1): tensor-memory lane n2 holds Re and Im of Y[k1][n2] in
+// adjacent columns.  The twiddle W8192^(n2 k1) and the fine part of the
+// fractional-sample-delay correction, fsubt[k1], are applied on the CUDA cores
 // while the result moves from tensor memory to shared memory as the A operand of
-// step 2, D3 (128 x 128) = A3 (128 x 256) B3^T: rows of A3 are (pol, k1), K =
-// [Re Y' over n2 | Im Y' over n2], and B3 is the real form of the first 64 rows
-// of DFT128 (row 2 k2 gives Re X, 2 k2 + 1 gives Im X; real data keeps channels
-// k < 4096, i.e. k2 < 64).  The fractional-sample-delay correction, the output
-// scale and the cast are applied as D3 leaves tensor memory.
+// step 2; both are geometric in k1, so one thread per (pol, n2) advances their
+// product by one complex multiply per k1.  Step 2 is D3 (128 x 128) = A3 (128 x
+// 256) B3^T: rows of A3 are (pol, k1), K = [Re Y' over n2 | Im Y' over n2], and
+// B3 is the real form of the first 64 rows of DFT128 (row 2 k2 gives Re X,
+// 2 k2 + 1 gives Im X; real data keeps channels k < 4096, i.e. k2 < 64).  The
+// coarse frac-delay factor fstept[k2], the output scale and the cast are applied
+// as D3 leaves tensor memory.
 //
 // Operands are FP16 (kind::f16) with FP32 accumulation in tensor memory.  The
 // FFT then carries four FP16 roundings (the rotated samples, both DFT matrices and
@@ -25,7 +29,7 @@
 // indices: with stride 64 and substride 128 (fxkernel.cpp:57-64), sample n has
 // rotator tsub[n2] * tstep[n1] and channel k frac-delay fsubt[k1] * fstept[k2].
 //
-// One persistent CTA of 512 threads per SM (186 KB of shared memory) loops over the windows of
+// One persistent CTA of 512 threads per SM (about 180 KB of shared memory) loops over the windows of
 // the block, both polarisations of a window at a time (they share the geometry,
 // the staged packed bytes, the rotator and the frac-delay tables, and fill the
 // 128 rows of step 2).  The next window's packed bytes, geometry and tables load
@@ -52,20 +56,18 @@ constexpr int KB = 128 * 128;                       // one 128-row SW128 K-block
 constexpr int OFF_A1 = 0;                  // DFT64, 2 K-blocks
 constexpr int OFF_B3 = OFF_A1 + 2 * KB;    // DFT128 rows k2 < 64, 4 K-blocks
 constexpr int OFF_BUF = OFF_B3 + 4 * KB;   // B1 of pol 0 (2 K-blocks), B1 of pol 1 (2); later A3 (4)
-constexpr int OFF_THI = OFF_BUF + 4 * KB;  // W8192^(16 j k1), [j < 8][k1]
-constexpr int OFF_TLO = OFF_THI + 64 * 8 * 8;    // W8192^(i k1), [i < 16][k1]
-constexpr int CONST_BYTES = OFF_TLO + 64 * 16 * 8 - OFF_A1;  // the part copied from the table image
+constexpr int CONST_BYTES = OFF_BUF - OFF_A1;  // the part copied from the table image (A1, B3)
 // two staging buffers (window w and the next one): tables tsub[128], tstep[64], fsubt[64],
 // fstept[64]; the packed window (2 pols, 2 bits) + 16-byte rounding; the geometry records
 constexpr int TAB_BYTES = (SUB + STRIDE + FSUB + STRIDE) * 8;
-constexpr int OFF_TAB = OFF_TLO + 64 * 16 * 8;
+constexpr int OFF_TAB = OFF_BUF + 4 * KB;
 constexpr int STAGE_BYTES = F / 2 + 64;
 constexpr int OFF_STAGE = OFF_TAB + 2 * TAB_BYTES;
 constexpr int OFF_GEOM = OFF_STAGE + 2 * STAGE_BYTES;
 constexpr int SMEM_BYTES = OFF_GEOM + 2 * (int)sizeof(Geom) + 1024;  // + alignment slack
-// global table image: A1 and B3 in their swizzled shared-memory layout, then THI and TLO
+// global table image: A1 and B3 in their swizzled shared-memory layout
 constexpr int TABLE_BYTES = CONST_BYTES;
-static_assert(OFF_BUF - OFF_B3 == 4 * KB && (OFF_THI - OFF_A1) % 16 == 0 && CONST_BYTES % 16 == 0, "layout");
+static_assert(OFF_BUF - OFF_B3 == 4 * KB && CONST_BYTES % 16 == 0, "layout");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
 
 struct Params {
@@ -75,6 +77,7 @@ struct Params {
   void *chan;
   float out_scale;
   const float *cscale;  // FP8 output: per-channel scale [nchan] (replaces out_scale), or null
+  float2 *probe;        // decode probe (DBG kernels): [nant][2][nfft][F] decoded samples
   int *err;
 };
 
@@ -126,7 +129,8 @@ __device__ __forceinline__ void stage_window(const Params &p, int w, unsigned ch
   }
 }
 
-template <typename OutT>
+// DBG = true (decode probe): every decoded sample is also written to p.probe before the rotation.
+template <typename OutT, bool DBG = false>
 __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
   using namespace tc;
   extern __shared__ unsigned char smem_raw[];
@@ -136,8 +140,6 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
   const uint32_t sbase = smem_u32(smem);
   const Job &job = p.job;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const float2 *thi = reinterpret_cast<const float2 *>(smem + OFF_THI);
-  const float2 *tlo = reinterpret_cast<const float2 *>(smem + OFF_TLO);
   const int nstreams = 2 * job.nant;
   const size_t ctile_stride = (size_t)p.T * nstreams * CW;
   OutT *chan = reinterpret_cast<OutT *>(p.chan);
@@ -164,6 +166,19 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
+
+  // twiddle-epilogue role of this thread: TMEM lane quarter q1 (n2 = 32 q1 + lane), warp group
+  // wg1 = (half of the k1 range) * 2 + pol; W8192^n2 and W8192^(32 half n2), once per CTA
+  const int q1 = warp & 3, wg1 = warp >> 2, tn2 = 32 * q1 + lane;
+  float2 tw_step, tw_base;
+  {
+    float sn, cs;
+    sincospif(-(float)tn2 / 4096.0f, &sn, &cs);
+    tw_step = make_float2(cs, sn);
+    sincospif(-(float)((wg1 >> 1) * tn2) / 128.0f, &sn, &cs);
+    tw_base = make_float2(cs, sn);
+  }
+  static_assert(NWG == 4, "four warp groups: two pols x two halves of k1");
 
   int phase = 0;    // windows correlated so far: the mbarriers' phase parity
   int pending = 0;  // 1: MMA1 issued and not yet waited for; 3: MMA3
@@ -212,6 +227,11 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
             const int byte = bp[64 * (i + u)];
             const float2 rot = cmul(rs, tstep[n1]);
             const float l0 = level2bit((byte >> sh0) & 3), l1 = level2bit((byte >> sh1) & 3);
+            if constexpr (DBG) {
+              const size_t pi = (((size_t)ant * 2) * job.nfft + (p.t0 + tl)) * F + n2 + 128 * n1;
+              p.probe[pi] = make_float2(l0, 0.f);
+              p.probe[pi + (size_t)job.nfft * F] = make_float2(l1, 0.f);
+            }
             x0[u] = make_float2(l0 * rot.x, l0 * rot.y);
             x1[u] = make_float2(l1 * rot.x, l1 * rot.y);
           }
@@ -229,7 +249,8 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
     }
     fence_proxy_async_smem();
     __syncthreads();
-    // ---- step 1: D1_pol (TMEM columns 128 pol ..) = A1 B1_pol^T, K = 128
+    // ---- step 1: D1_pol (TMEM columns 128 pol ..) = B1_pol A1^T, K = 128: lane n2, column
+    //      2 k1 + part, so a thread holds Re and Im of Y[k1][n2] for its n2 in adjacent columns
     if (tid == 0) {
       tc_fence_after();
 #pragma unroll
@@ -237,8 +258,8 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
 #pragma unroll
         for (int kk = 0; kk < 8; kk++) {
           const uint32_t o = (uint32_t)((kk >> 2) * KB + (kk & 3) * 32);
-          mma_f16(tmem + 128 * pol, desc_sw128(sbase + OFF_A1 + o),
-                  desc_sw128(sbase + OFF_BUF + pol * 2 * KB + o), IDESC, kk > 0 ? 1u : 0u);
+          mma_f16(tmem + 128 * pol, desc_sw128(sbase + OFF_BUF + pol * 2 * KB + o),
+                  desc_sw128(sbase + OFF_A1 + o), IDESC, kk > 0 ? 1u : 0u);
         }
       mma_commit(smem_u32(&bar_mma1));
     }
@@ -253,40 +274,36 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
     }
     pending = 0;
     tc_fence_after();
-    // ---- twiddle, FP16, into A3 (rows pol*64 + k1, K = [Re Y' n2 0..127 | Im Y' n2 0..127]);
-    //      warp group wg takes pol wg & 1 and half wg >> 1 of the n2 columns
+    // ---- twiddle and fine frac-delay, FP16, into A3 (rows pol*64 + k1, K = [Re Y' n2 0..127 |
+    //      Im Y' n2 0..127]).  Thread (pol, n2, half) takes k1 = 32 half .. 32 half + 31 of its row:
+    //      Y'[k1][n2] = Y[k1][n2] W8192^(n2 k1) fsubt[k1] = Y[k1][n2] w0 r^(k1 - 32 half), with
+    //      r = W8192^n2 e^(2 pi i cf) (fsubt is geometric in k1), so the factor advances by one
+    //      complex multiply per k1 (over 32 steps its rounding grows to ~3e-6, far below FP16's).
+    //      Multiplying row k1 by fsubt[k1] before step 2 scales X[k1 + 64 k2] by it for every k2.
     {
-      const int q = warp & 3, wg = warp >> 2, pol = wg & 1;
-      const int c = 32 * q + lane, k1 = c >> 1, part = c & 1;
-      const int m = pol * 64 + k1;
-      constexpr int JPER = 8 / (NWG / 2);
+      const int pol = wg1 & 1, half = wg1 >> 1;
+      const float2 fs1 = fsubt[1], fs0 = fsubt[32 * half];
+      float2 r = cmul(tw_step, fs1), wk = cmul(tw_base, fs0);
+      // byte offsets of the K positions n2 (Re) and 128 + n2 (Im) in row m = pol*64 + k1, for
+      // the eight k1 & 7: rows of one 8-row group differ in the swizzle of their chunk index
+      const int kc = tn2 & 63, kbase = OFF_BUF + (tn2 >> 6) * KB + (kc & 7) * 2;
+      uint32_t xo[8];
+#pragma unroll
+      for (int e = 0; e < 8; e++) xo[e] = (uint32_t)(kbase + e * 128 + ((((kc >> 3) ^ e) & 7) << 4));
 #pragma unroll 1
-      for (int j = (wg >> 1) * JPER; j < (wg >> 1) * JPER + JPER; j++) {
-        float v[16], pv[16];
-        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(128 * pol + 16 * j), v);
+      for (int jj = 0; jj < 4; jj++) {
+        const int k10 = 32 * half + 8 * jj;  // first k1 of the chunk (a multiple of 8)
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * q1) << 16) + (uint32_t)(128 * pol + 2 * k10), v);
+        unsigned char *row0 = smem + (pol * 64 + k10) * 128;
 #pragma unroll
-        for (int i = 0; i < 16; i++) pv[i] = __shfl_xor_sync(0xffffffffu, v[i], 1);
-        const float2 wh = thi[j * 64 + k1];
-        uint32_t h[8];
-#pragma unroll
-        for (int i = 0; i < 16; i += 2) {
-          float y[2];
-#pragma unroll
-          for (int u = 0; u < 2; u++) {
-            const float2 tw = cmul(wh, tlo[(i + u) * 64 + k1]);
-            const float yr = part ? pv[i + u] : v[i + u], yi = part ? v[i + u] : pv[i + u];
-            y[u] = part ? fmaf(yr, tw.y, yi * tw.x) : fmaf(yr, tw.x, -(yi * tw.y));
-          }
-          h[i >> 1] = pack_h2(y[0], y[1]);
+        for (int e = 0; e < 8; e++) {
+          const float2 y = cmul(make_float2(v[2 * e], v[2 * e + 1]), wk);
+          wk = cmul(wk, r);
+          const uint32_t h = pack_h2(y.x, y.y);
+          *reinterpret_cast<uint16_t *>(row0 + xo[e]) = (uint16_t)(h & 0xFFFFu);
+          *reinterpret_cast<uint16_t *>(row0 + xo[e] + 2 * KB) = (uint16_t)(h >> 16);
         }
-        // the two threads of a row store to the same positions of different K-blocks: they
-        // write their two chunks in opposite orders so the 8-thread store phases see 8 banks
-        const int kb = part * 2 + (j >> 2), o0 = 2 * (j & 3);
-        unsigned char *row = smem + OFF_BUF + kb * KB + m * 128;
-        const uint4 c0 = make_uint4(h[0], h[1], h[2], h[3]), c1 = make_uint4(h[4], h[5], h[6], h[7]);
-        const int oa = o0 + part, ob = o0 + 1 - part;
-        *reinterpret_cast<uint4 *>(row + ((oa ^ (m & 7)) << 4)) = part ? c1 : c0;
-        *reinterpret_cast<uint4 *>(row + ((ob ^ (m & 7)) << 4)) = part ? c0 : c1;
       }
     }
     fence_proxy_async_smem();
@@ -316,7 +333,6 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
     {
       const int q = warp & 3, wg = warp >> 2;
       const int m = 32 * q + lane, pol = m >> 6, k1 = m & 63;
-      const float2 fs = fsubt[k1];
       const float sc = p.out_scale;
       OutT *o = out0 + (size_t)pol * CW + (k1 & 15);
       constexpr int CPER = 128 / NWG;
@@ -328,8 +344,7 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
 #pragma unroll
         for (int e = 0; e < 8; e++) {
           const int k2 = (col0 >> 1) + e, k = k1 + 64 * k2;
-          const float2 fr = cmul(fs, fstept[k2]);
-          const float2 z = cmul(make_float2(v[2 * e], v[2 * e + 1]), fr);
+          const float2 z = cmul(make_float2(v[2 * e], v[2 * e + 1]), fstept[k2]);  // fsubt[k1] is in A3
           o[(size_t)(k >> 4) * ctile_stride] = to_out<OutT>(z, chan_scale<OutT>(p.cscale, k, sc));
         }
       }
@@ -386,25 +401,13 @@ cudaError_t make_fstage_tc_tables(void **out) {
       put(OFF_B3, kb, 2 * k2 + 1, k, -sn);
       put(OFF_B3, kb + 2, 2 * k2 + 1, k, cs);
     }
-  float2 *th = reinterpret_cast<float2 *>(&img[(size_t)OFF_THI]);
-  float2 *tl = reinterpret_cast<float2 *>(&img[(size_t)OFF_TLO]);
-  for (int k1 = 0; k1 < N1; k1++) {
-    for (int j = 0; j < 8; j++) {
-      const double a = -2.0 * pi * (double)((16 * j * k1) % F) / (double)F;
-      th[j * 64 + k1] = make_float2((float)cos(a), (float)sin(a));
-    }
-    for (int i = 0; i < 16; i++) {
-      const double a = -2.0 * pi * (double)((i * k1) % F) / (double)F;
-      tl[i * 64 + k1] = make_float2((float)cos(a), (float)sin(a));
-    }
-  }
   cudaError_t e = cudaMalloc(out, img.size());
   if (e != cudaSuccess) return e;
   return cudaMemcpy(*out, img.data(), img.size(), cudaMemcpyHostToDevice);
 }
 
 cudaError_t launch_fstage_tc(const Job &job, const void *tables, int t0, int nt, int T, void *chan, int chan_type,
-                             float out_scale, cudaStream_t s, const float *cscale) {
+                             float out_scale, cudaStream_t s, const float *cscale, float2 *probe) {
   using namespace ftc;
   if (nt <= 0) return cudaSuccess;
   if (!fstage_tc_supported(job, chan_type) || !tables) return cudaErrorInvalidValue;
@@ -417,6 +420,7 @@ cudaError_t launch_fstage_tc(const Job &job, const void *tables, int t0, int nt,
   p.chan = chan;
   p.out_scale = out_scale;
   p.cscale = cscale;
+  p.probe = probe;
   cudaError_t e = cudaGetSymbolAddress((void **)&p.err, g_ftc_err);
   if (e != cudaSuccess) return e;
   int dev = 0, nsm = 0;
@@ -425,18 +429,15 @@ cudaError_t launch_fstage_tc(const Job &job, const void *tables, int t0, int nt,
   if (e != cudaSuccess) return e;
   const long long nwin = (long long)nt * job.nant;
   const unsigned grid = (unsigned)(nwin < nsm ? nwin : nsm);
-  if (chan_type == CHAN_F8) {
-    auto kern = fstage_tc_kernel<__nv_fp8x2_e4m3>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    if (e != cudaSuccess) return e;
+  auto launch = [&](auto kern) -> cudaError_t {
+    cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e2 != cudaSuccess) return e2;
     kern<<<grid, NT, SMEM_BYTES, s>>>(p);
-  } else {
-    auto kern = fstage_tc_kernel<__half2>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    kern<<<grid, NT, SMEM_BYTES, s>>>(p);
-  }
-  return cudaGetLastError();
+    return cudaGetLastError();
+  };
+  if (chan_type == CHAN_F8)
+    return probe ? launch(fstage_tc_kernel<__nv_fp8x2_e4m3, true>) : launch(fstage_tc_kernel<__nv_fp8x2_e4m3>);
+  return probe ? launch(fstage_tc_kernel<__half2, true>) : launch(fstage_tc_kernel<__half2>);
 }
 
 // Reads and clears the error flag of the tensor-core F-stage (a bounded wait expired).

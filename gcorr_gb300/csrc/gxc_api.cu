@@ -238,6 +238,7 @@ const char *gxc_last_error(const gxc_handle *h) { return h ? h->err.c_str() : "n
 int gxc_last_launch_count(const gxc_handle *h) { return h ? h->launches : 0; }
 int gxc_fft_block(const gxc_handle *h) { return h ? h->T : 0; }
 int gxc_num_blocks(const gxc_handle *h) { return h ? h->nblocks : 0; }
+int gxc_fft_engine(const gxc_handle *h) { return h && h->tc_fstage ? GXC_FFT_TENSOR : GXC_FFT_CUDA_CORE; }
 const float *gxc_device_visibilities(const gxc_handle *h) { return h ? (const float *)h->d_vis : nullptr; }
 
 static void release(gxc_handle *h) {
@@ -393,7 +394,10 @@ gxc_status gxc_create(const gxc_config *cfg, gxc_handle **out) {
   if (e == cudaSuccess) e = make_tile_pairs(nant, &h->d_pairs);
   // the tensor-core F-stage runs when asked for; AUTO keeps the CUDA-core FFT, which measured
   // faster (16 antennas, nchan 4096, FP16: F-stage 41.1 ms against 44.4 ms per sub-integration)
-  h->tc_fstage = cfg->fft_engine == GXC_FFT_TENSOR && fstage_tc_supported(j, h->chan_type);
+  // AUTO takes the tensor-core F-stage where it runs (8192-point 2-bit real windows, FP16 or
+  // FP8 channelised data): 36.2 ms against 40.1 ms for the CUDA-core FFT per second of the
+  // 16-antenna, 512 Ms/s workload at FP16
+  h->tc_fstage = cfg->fft_engine != GXC_FFT_CUDA_CORE && fstage_tc_supported(j, h->chan_type);
   if (e == cudaSuccess && h->tc_fstage) e = make_fstage_tc_tables(&h->d_tc_tables);
   if (h->chan_type == CHAN_F8 && cfg->fp8_scaling == GXC_FP8_SCALE_CHANNEL) {
     // calibration block: up to 64 FFTs, at most 256 MB of FP32 channelised data (at least 4 FFTs)
@@ -820,7 +824,11 @@ gxc_status gxc_probe_unpack(gxc_handle *h, float *decoded) {
   for (int b = 0; e == cudaSuccess && b < h->nblocks; b++) {
     const int t0 = b * h->T;
     const int nt = (c.nfft - t0) < h->T ? (c.nfft - t0) : h->T;
-    e = launch_fstage_probe(h->job, h->d_tw, t0, nt, h->T, chan, h->chan_type, h->out_scale, probe, nullptr);
+    // the probe runs the handle's own F-stage kernel family
+    e = h->tc_fstage ? launch_fstage_tc(h->job, h->d_tc_tables, t0, nt, h->T, chan, h->chan_type, h->out_scale,
+                                        nullptr, nullptr, probe)
+                     : launch_fstage_probe(h->job, h->d_tw, t0, nt, h->T, chan, h->chan_type, h->out_scale, probe,
+                                           nullptr);
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(decoded, probe, n * sizeof(float2), cudaMemcpyDefault);

@@ -75,8 +75,10 @@ cudaError_t launch_fstage_probe(const Job &job, const float2 *twiddles, int t0, 
 // fstage_tc.cu: the tensor-core F-stage (8192-point windows, 2-bit real, FP16 / FP8 output).
 int fstage_tc_supported(const Job &job, int chan_type);
 cudaError_t make_fstage_tc_tables(void **out);  // its constant operands (cudaMalloc'd; caller frees)
+// probe non-null: the decode probe (every decoded sample also written to probe [nant][2][nfft][F]).
 cudaError_t launch_fstage_tc(const Job &job, const void *tables, int t0, int nt, int T, void *chan, int chan_type,
-                             float out_scale, cudaStream_t s, const float *cscale = nullptr);
+                             float out_scale, cudaStream_t s, const float *cscale = nullptr,
+                             float2 *probe = nullptr);
 cudaError_t fstage_tc_take_error(int *flag);
 
 // xstage_fp32.cu: accumulates visibilities of FFTs [0, nt) of the block into

@@ -193,6 +193,11 @@ class FxKernel:
         return int(L.lib().gxc_fft_block(self._h))
 
     @property
+    def fft_engine_used(self) -> str:
+        """The F-stage engine this handle runs ("tensor" or "cuda_core"; "auto" resolved)."""
+        return "tensor" if L.lib().gxc_fft_engine(self._h) == L.GXC_FFT_TENSOR else "cuda_core"
+
+    @property
     def num_blocks(self) -> int:
         """F/X passes of the last process() (one more than nfft / fft_block when host inputs start
         with a short block)."""

@@ -59,9 +59,9 @@ enum { GXC_XENGINE_AUTO = 0, GXC_XENGINE_CUDA_CORE = 1, GXC_XENGINE_TENSOR = 2 }
 /* F-stage FFT engine.  TENSOR: the FFT as two dense DFT products on tcgen05 (FP16
  * operands, FP32 accumulation), for FP16 / FP8 channelised output of 8192-point
  * windows of 2-bit real data (nchan 4096); it adds four FP16 roundings inside the
- * FFT.  CUDA_CORE: the FP32 register FFT of every shape.  AUTO: CUDA_CORE, which is
- * the faster of the two on GB300 (16 antennas, nchan 4096, FP16: 41.1 against
- * 44.4 ms per sub-integration). */
+ * FFT.  CUDA_CORE: the FP32 register FFT of every shape.  AUTO: TENSOR where it
+ * runs, the faster of the two on GB300 (16 antennas, nchan 4096, FP16: 36.2 against
+ * 40.1 ms per sub-integration), else CUDA_CORE. */
 enum { GXC_FFT_AUTO = 0, GXC_FFT_CUDA_CORE = 1, GXC_FFT_TENSOR = 2 };
 /* FFT-range split of the FP16 / FP8 tensor-core X-stage: each channel group's FFTs of a block go to
  * two CTAs, the second accumulating into a second plane that finalisation adds.  AUTO: split when
@@ -179,6 +179,8 @@ int gxc_fft_block(const gxc_handle *h);
    host and the block was chosen, the passes cover 4096, 8192, ... FFTs up to the block (the
    compute starts after a shorter copy), which can add passes. */
 int gxc_num_blocks(const gxc_handle *h);
+/* F-stage engine this handle runs: GXC_FFT_TENSOR or GXC_FFT_CUDA_CORE (AUTO resolved). */
+int gxc_fft_engine(const gxc_handle *h);
 
 /* Stage timing: when enabled, process() records CUDA events around the F-stage
  * and X-stage launches; gxc_stage_times returns the summed milliseconds of the

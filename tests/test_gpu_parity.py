@@ -178,9 +178,9 @@ def test_fp16_channelised_vs_fp64():
 @pytest.mark.parametrize("is_complex", [True, False])
 @pytest.mark.parametrize("precision", ["fp16", "fp8"])
 def test_large_fft_reduced_precision_vs_fp64(fft_len, is_complex, precision):
-    """8192-point windows go through the packed-pair F-stage; 16384- and 32768-point windows with
-    FP16 or FP8 channelised data through the F-stage whose intermediate spectrum is held in FP16
-    shared memory (two extra 2^-11 roundings).
+    """8192-point windows go through the tensor-core F-stage (2-bit real) or the packed-pair one
+    (8-bit complex); 16384- and 32768-point windows with FP16 or FP8 channelised data through the
+    F-stage whose intermediate spectrum is held in FP16 shared memory (two extra 2^-11 roundings).
     FP16 must stay within the FP16 tolerance of the FP64 oracle.  FP8: crosses within 6 % (the
     E4M3 bound of the other FP8 tests); the power spectra's E4M3 rounding error only averages
     over the 8 FFTs here (1 % holds for 200 FFTs; about 2.3 % is expected for 8), bound 3.5 %."""

@@ -8,8 +8,9 @@ FFT starts from.  Each case compares them with the oracle's restatement of
 itself pinned to the level table in tests/golden/lut2bit.npy, and with the
 8-bit complex layout (int8 A.re, A.im, B.re, B.im per time sample): every
 float's bits must match, for every kernel family (256..32768 points, FP32 and
-FP16-buffer kernels), at odd and even window offsets, with all 256 byte values
-inside the decoded windows.  Flagged windows must stay untouched.
+FP16-buffer kernels, and the tensor-core F-stage of 8192-point 2-bit windows),
+at odd and even window offsets, with all 256 byte values inside the decoded
+windows.  Flagged windows must stay untouched.
 """
 import ctypes as C
 
@@ -25,13 +26,16 @@ pytestmark = pytest.mark.gpu
 BW = 64e6
 NANT, NFFT = 3, 4
 
-# (FFT length, complex, precision): one case per kernel family and input format
+# (FFT length, complex, precision, F-stage engine): one case per kernel family and input format.
+# 8192-point 2-bit FP16 / FP8 runs the tensor-core F-stage by default (its own decode loop).
 CASES = [
-    (256, False, "fp32"), (2048, False, "fp32"), (4096, False, "fp16"), (8192, False, "fp32"),
-    (8192, False, "fp8"), (16384, False, "fp32"), (16384, False, "fp16"), (32768, False, "fp32"),
-    (32768, False, "fp16"),
-    (256, True, "fp32"), (1024, True, "fp32"), (8192, True, "fp32"), (16384, True, "fp32"),
-    (16384, True, "fp16"), (32768, True, "fp32"), (32768, True, "fp8"),
+    (256, False, "fp32", "auto"), (2048, False, "fp32", "auto"), (4096, False, "fp16", "auto"),
+    (8192, False, "fp32", "auto"), (8192, False, "fp8", "auto"), (8192, False, "fp16", "auto"),
+    (8192, False, "fp16", "cuda_core"), (16384, False, "fp32", "auto"), (16384, False, "fp16", "auto"),
+    (32768, False, "fp32", "auto"), (32768, False, "fp16", "auto"),
+    (256, True, "fp32", "auto"), (1024, True, "fp32", "auto"), (8192, True, "fp32", "auto"),
+    (16384, True, "fp32", "auto"), (16384, True, "fp16", "auto"), (32768, True, "fp32", "auto"),
+    (32768, True, "fp8", "auto"),
 ]
 
 
@@ -53,12 +57,13 @@ def _inputs(nbytes, seed):
             for _ in range(NANT)]
 
 
-@pytest.mark.parametrize("F,is_complex,precision", CASES)
-def test_gpu_unpack_bit_exact(F, is_complex, precision):
+@pytest.mark.parametrize("F,is_complex,precision,fft_engine", CASES)
+def test_gpu_unpack_bit_exact(F, is_complex, precision, fft_engine):
     import torch
     nchan = F if is_complex else F // 2
     nbit = 8 if is_complex else 2
-    fx = FxKernel(NANT, nchan, NFFT, nbit, 8.4e9, BW, is_complex, precision=precision, device=0)
+    fx = FxKernel(NANT, nchan, NFFT, nbit, 8.4e9, BW, is_complex, precision=precision, device=0,
+                  fft_engine=fft_engine)
     try:
         inputs = _inputs(fx.bytes_per_antenna, seed=F + int(is_complex))
         dev = [torch.from_numpy(x).cuda() for x in inputs]
