@@ -53,19 +53,20 @@ constexpr int NT = 512;                             // 16 warps: 4 groups of the
 constexpr int NWG = NT / 128;
 constexpr int KB = 128 * 128;                       // one 128-row SW128 K-block (64 FP16 K-elements)
 // shared-memory image (byte offsets from a 1024-aligned base)
-constexpr int OFF_A1 = 0;                  // DFT64, 2 K-blocks
-constexpr int OFF_B3 = OFF_A1 + 2 * KB;    // DFT128 rows k2 < 64, 4 K-blocks
-constexpr int OFF_BUF = OFF_B3 + 4 * KB;   // B1 of pol 0 (2 K-blocks), B1 of pol 1 (2); later A3 (4)
-constexpr int CONST_BYTES = OFF_BUF - OFF_A1;  // the part copied from the table image (A1, B3)
+constexpr int OFF_A1 = 0;                  // the window's A1 (DFT64 times tstep), 1 K-block
+constexpr int OFF_B3 = OFF_A1 + KB;        // DFT128 rows k2 < 64, 4 K-blocks (constant)
+constexpr int OFF_BUF = OFF_B3 + 4 * KB;   // B1 of pol 0 (1 K-block), B1 of pol 1 (1); later A3 (4)
+constexpr int CONST_BYTES = 4 * KB;        // the part copied from the table image (B3)
+constexpr int OFF_W64 = OFF_BUF + 4 * KB;  // W64^j = exp(-2 pi i j / 64), j < 64 (float2)
 // two staging buffers (window w and the next one): tables tsub[128], tstep[64], fsubt[64],
 // fstept[64]; the packed window (2 pols, 2 bits) + 16-byte rounding; the geometry records
 constexpr int TAB_BYTES = (SUB + STRIDE + FSUB + STRIDE) * 8;
-constexpr int OFF_TAB = OFF_BUF + 4 * KB;
+constexpr int OFF_TAB = OFF_W64 + 64 * 8;
 constexpr int STAGE_BYTES = F / 2 + 64;
 constexpr int OFF_STAGE = OFF_TAB + 2 * TAB_BYTES;
 constexpr int OFF_GEOM = OFF_STAGE + 2 * STAGE_BYTES;
 constexpr int SMEM_BYTES = OFF_GEOM + 2 * (int)sizeof(Geom) + 1024;  // + alignment slack
-// global table image: A1 and B3 in their swizzled shared-memory layout
+// global table image: B3 in its swizzled shared-memory layout
 constexpr int TABLE_BYTES = CONST_BYTES;
 static_assert(OFF_BUF - OFF_B3 == 4 * KB && CONST_BYTES % 16 == 0, "layout");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
@@ -91,6 +92,15 @@ __host__ __device__ inline int sw128_off(int row, int k) {
 __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
   const __half2 h = __floats2half2_rn(a, b);
   return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// FP16 levels of two 2-bit codes, packed (a low, b high): the level table of fxkernel.cpp:17-18
+// {-HiMag, -1, 1, HiMag} as FP16 bit patterns, code c at bytes 2c, 2c+1 of {kHi:kLo}, picked by
+// one byte permute.  HiMag = 3.3359 is 3.3359375 in FP16, the nearest half.
+__device__ __forceinline__ uint32_t level_pair_h2(int a, int b) {
+  constexpr uint32_t kLo = 0xBC00C2ACu, kHi = 0x42AC3C00u;  // codes 1, 0 | codes 3, 2
+  const uint32_t sel = (uint32_t)(a * 0x22 + 0x10) | ((uint32_t)(b * 0x22 + 0x10) << 8);
+  return tc::prmt(kLo, kHi, sel);
 }
 
 // Stages window w into buffer b: its geometry record, the packed bytes (asynchronous 16-byte
@@ -144,11 +154,17 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
   const size_t ctile_stride = (size_t)p.T * nstreams * CW;
   OutT *chan = reinterpret_cast<OutT *>(p.chan);
 
-  // constant operands and twiddles, once per CTA
+  // constant operand B3 and the DFT64 roots, once per CTA
   {
-    uint4 *dst = reinterpret_cast<uint4 *>(smem + OFF_A1);
+    uint4 *dst = reinterpret_cast<uint4 *>(smem + OFF_B3);
     for (int i = tid; i < CONST_BYTES / 16; i += NT) dst[i] = __ldg(&p.tables[i]);
+    if (tid < 64) {
+      float sn, cs;
+      sincospif(-(float)tid / 32.0f, &sn, &cs);
+      reinterpret_cast<float2 *>(smem + OFF_W64)[tid] = make_float2(cs, sn);
+    }
   }
+  const float2 *w64 = reinterpret_cast<const float2 *>(smem + OFF_W64);
   if (tid == 0) {
     mbar_init(smem_u32(&bar_mma1), 1);
     mbar_init(smem_u32(&bar_mma3), 1);
@@ -207,60 +223,74 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
     const float2 *tsub = reinterpret_cast<const float2 *>(smem + OFF_TAB + b * TAB_BYTES);
     const float2 *tstep = tsub + SUB, *fsubt = tstep + STRIDE, *fstept = fsubt + FSUB;
     const int off = g.offset;
-    // ---- decode + fringe-rotate into B1 of both pols: task (n2, o) covers n1 = 8o..8o+7
+    // ---- decode into B1 of both pols and build the window's A1.  The rotator of sample
+    //      n = n2 + 128 n1 is tsub[n2] tstep[n1]: tstep[n1] goes into A1 (row 2 k1 + part, column
+    //      n1: Re / Im of W64^(n1 k1) tstep[n1], one FP16 rounding), tsub[n2] into the twiddle
+    //      epilogue, so B1 holds the real levels (B1_pol[n2][n1], K = n1) and step 1 needs K = 64.
     {
       const int sbase = (int)(((long long)off >> 1) - (((long long)off >> 1) & ~15LL));
 #pragma unroll 1
-      for (int task = tid; task < N2 * 8; task += NT) {
+      for (int task = tid; task < N2 * 8; task += NT) {  // (n2, o): n1 = 8o .. 8o+7
         const int n2 = task & (N2 - 1), o = task >> 7;
         const int p0 = (off & 1) + n2;  // sample index relative to byte off/2
         const unsigned char *bp = stage + sbase + (p0 >> 1) + 64 * (8 * o);
         const int sh0 = 2 * (2 * (p0 & 1)), sh1 = sh0 + 2;
-        const float2 rs = tsub[n2];
-        uint32_t re0[4], im0[4], re1[4], im1[4];
+        uint32_t h0[4], h1[4];
 #pragma unroll
         for (int i = 0; i < 8; i += 2) {
-          float2 x0[2], x1[2];
-#pragma unroll
-          for (int u = 0; u < 2; u++) {
-            const int n1 = 8 * o + i + u;
-            const int byte = bp[64 * (i + u)];
-            const float2 rot = cmul(rs, tstep[n1]);
-            const float l0 = level2bit((byte >> sh0) & 3), l1 = level2bit((byte >> sh1) & 3);
-            if constexpr (DBG) {
-              const size_t pi = (((size_t)ant * 2) * job.nfft + (p.t0 + tl)) * F + n2 + 128 * n1;
-              p.probe[pi] = make_float2(l0, 0.f);
-              p.probe[pi + (size_t)job.nfft * F] = make_float2(l1, 0.f);
-            }
-            x0[u] = make_float2(l0 * rot.x, l0 * rot.y);
-            x1[u] = make_float2(l1 * rot.x, l1 * rot.y);
+          const int ba = bp[64 * i], bb = bp[64 * (i + 1)];
+          const int ca0 = (ba >> sh0) & 3, cb0 = (bb >> sh0) & 3, ca1 = (ba >> sh1) & 3, cb1 = (bb >> sh1) & 3;
+          h0[i >> 1] = level_pair_h2(ca0, cb0);
+          h1[i >> 1] = level_pair_h2(ca1, cb1);
+          if constexpr (DBG) {
+            const float la0 = level2bit(ca0), lb0 = level2bit(cb0), la1 = level2bit(ca1), lb1 = level2bit(cb1);
+            const size_t pi = (((size_t)ant * 2) * job.nfft + (p.t0 + tl)) * F + n2 + 128 * (8 * o + i);
+            const size_t pp = (size_t)job.nfft * F;  // pol 1
+            p.probe[pi] = make_float2(la0, 0.f);
+            p.probe[pi + 128] = make_float2(lb0, 0.f);
+            p.probe[pi + pp] = make_float2(la1, 0.f);
+            p.probe[pi + pp + 128] = make_float2(lb1, 0.f);
           }
-          re0[i >> 1] = pack_h2(x0[0].x, x0[1].x);
-          im0[i >> 1] = pack_h2(x0[0].y, x0[1].y);
-          re1[i >> 1] = pack_h2(x1[0].x, x1[1].x);
-          im1[i >> 1] = pack_h2(x1[0].y, x1[1].y);
         }
         const int so = n2 * 128 + ((o ^ (n2 & 7)) << 4);
-        *reinterpret_cast<uint4 *>(smem + OFF_BUF + 0 * KB + so) = make_uint4(re0[0], re0[1], re0[2], re0[3]);
-        *reinterpret_cast<uint4 *>(smem + OFF_BUF + 1 * KB + so) = make_uint4(im0[0], im0[1], im0[2], im0[3]);
-        *reinterpret_cast<uint4 *>(smem + OFF_BUF + 2 * KB + so) = make_uint4(re1[0], re1[1], re1[2], re1[3]);
-        *reinterpret_cast<uint4 *>(smem + OFF_BUF + 3 * KB + so) = make_uint4(im1[0], im1[1], im1[2], im1[3]);
+        *reinterpret_cast<uint4 *>(smem + OFF_BUF + 0 * KB + so) = make_uint4(h0[0], h0[1], h0[2], h0[3]);
+        *reinterpret_cast<uint4 *>(smem + OFF_BUF + 1 * KB + so) = make_uint4(h1[0], h1[1], h1[2], h1[3]);
+      }
+      // A1: thread (k1, c), k1 = tid % 64 (a warp reads one tstep entry and consecutive roots),
+      // writes columns n1 = 8c .. 8c+7 of rows 2 k1 (Re) and 2 k1 + 1 (Im).  tstep is geometric
+      // (tstep[n1] = tstep[1]^n1), so along n1 the entry advances by the factor tstep[1] W64^k1.
+      {
+        const int k1 = tid & 63, c = tid >> 6;
+        const float2 st = cmul(tstep[1], w64[k1]);
+        float2 a = cmul(tstep[8 * c], w64[(8 * c * k1) & 63]);
+        uint32_t hr[4], hi[4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          const float2 a1 = cmul(a, st);
+          hr[e >> 1] = pack_h2(a.x, a1.x);
+          hi[e >> 1] = pack_h2(a.y, a1.y);
+          a = cmul(a1, st);
+        }
+        const int r0 = 2 * k1, r1 = r0 + 1;
+        *reinterpret_cast<uint4 *>(smem + OFF_A1 + r0 * 128 + ((c ^ (r0 & 7)) << 4)) =
+            make_uint4(hr[0], hr[1], hr[2], hr[3]);
+        *reinterpret_cast<uint4 *>(smem + OFF_A1 + r1 * 128 + ((c ^ (r1 & 7)) << 4)) =
+            make_uint4(hi[0], hi[1], hi[2], hi[3]);
       }
     }
     fence_proxy_async_smem();
     __syncthreads();
-    // ---- step 1: D1_pol (TMEM columns 128 pol ..) = B1_pol A1^T, K = 128: lane n2, column
-    //      2 k1 + part, so a thread holds Re and Im of Y[k1][n2] for its n2 in adjacent columns
+    // ---- step 1: D1_pol (TMEM columns 128 pol ..) = B1_pol A1^T, K = 64: lane n2, column
+    //      2 k1 + part, so a thread holds Re and Im of Y[k1][n2] / tsub[n2] for its n2 in
+    //      adjacent columns
     if (tid == 0) {
       tc_fence_after();
 #pragma unroll
       for (int pol = 0; pol < 2; pol++)
 #pragma unroll
-        for (int kk = 0; kk < 8; kk++) {
-          const uint32_t o = (uint32_t)((kk >> 2) * KB + (kk & 3) * 32);
-          mma_f16(tmem + 128 * pol, desc_sw128(sbase + OFF_BUF + pol * 2 * KB + o),
-                  desc_sw128(sbase + OFF_A1 + o), IDESC, kk > 0 ? 1u : 0u);
-        }
+        for (int kk = 0; kk < 4; kk++)
+          mma_f16(tmem + 128 * pol, desc_sw128(sbase + OFF_BUF + pol * KB + kk * 32),
+                  desc_sw128(sbase + OFF_A1 + kk * 32), IDESC, kk > 0 ? 1u : 0u);
       mma_commit(smem_u32(&bar_mma1));
     }
     pending = 1;
@@ -283,7 +313,7 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
     {
       const int pol = wg1 & 1, half = wg1 >> 1;
       const float2 fs1 = fsubt[1], fs0 = fsubt[32 * half];
-      float2 r = cmul(tw_step, fs1), wk = cmul(tw_base, fs0);
+      float2 r = cmul(tw_step, fs1), wk = cmul(cmul(tw_base, fs0), tsub[tn2]);  // tsub: the rotator's n2 part
       // byte offsets of the K positions n2 (Re) and 128 + n2 (Im) in row m = pol*64 + k1, for
       // the eight k1 & 7: rows of one 8-row group differ in the swizzle of their chunk index
       const int kc = tn2 & 63, kbase = OFF_BUF + (tn2 >> 6) * KB + (kc & 7) * 2;
@@ -380,26 +410,16 @@ cudaError_t make_fstage_tc_tables(void **out) {
     const __half h = __double2half(v);
     memcpy(&img[(size_t)base + (size_t)kb * KB + (size_t)sw128_off(row, k)], &h, 2);
   };
-  // A1[c][K]: c = 2 k1 + part; K-block 0 multiplies Re x[n1], K-block 1 Im x[n1]
-  for (int k1 = 0; k1 < N1; k1++)
-    for (int n1 = 0; n1 < N1; n1++) {
-      const double th = 2.0 * pi * (double)((n1 * k1) % N1) / (double)N1;
-      const double cs = cos(th), sn = sin(th);
-      put(OFF_A1, 0, 2 * k1, n1, cs);
-      put(OFF_A1, 1, 2 * k1, n1, sn);
-      put(OFF_A1, 0, 2 * k1 + 1, n1, -sn);
-      put(OFF_A1, 1, 2 * k1 + 1, n1, cs);
-    }
   // B3[c3][K]: c3 = 2 k2 + part (k2 < 64); K-blocks 0,1: Re Y' n2 0..63, 64..127; 2,3: Im Y'
   for (int k2 = 0; k2 < N2 / 2; k2++)
     for (int n2 = 0; n2 < N2; n2++) {
       const double ps = 2.0 * pi * (double)((n2 * k2) % N2) / (double)N2;
       const double cs = cos(ps), sn = sin(ps);
       const int kb = n2 >> 6, k = n2 & 63;
-      put(OFF_B3, kb, 2 * k2, k, cs);
-      put(OFF_B3, kb + 2, 2 * k2, k, sn);
-      put(OFF_B3, kb, 2 * k2 + 1, k, -sn);
-      put(OFF_B3, kb + 2, 2 * k2 + 1, k, cs);
+      put(0, kb, 2 * k2, k, cs);
+      put(0, kb + 2, 2 * k2, k, sn);
+      put(0, kb, 2 * k2 + 1, k, -sn);
+      put(0, kb + 2, 2 * k2 + 1, k, cs);
     }
   cudaError_t e = cudaMalloc(out, img.size());
   if (e != cudaSuccess) return e;
