@@ -28,14 +28,19 @@
 // The rotator and frac-delay tables of the fxkernel layout fall on the four-step
 // indices: with stride 64 and substride 128 (fxkernel.cpp:57-64), sample n has
 // rotator tsub[n2] * tstep[n1] and channel k frac-delay fsubt[k1] * fstept[k2].
+// tstep[n1] is folded into a per-window A1 (Re / Im of W64^(n1 k1) tstep[n1]), so
+// B1 holds the real 2-bit levels and step 1 has K = 64; tsub[n2] joins the
+// twiddle recurrence.
 //
-// One persistent CTA of 512 threads per SM (about 180 KB of shared memory) loops over the windows of
-// the block, both polarisations of a window at a time (they share the geometry,
-// the staged packed bytes, the rotator and the frac-delay tables, and fill the
-// 128 rows of step 2).  The next window's packed bytes, geometry and tables load
-// into a second staging buffer while the current window's step-1 MMAs run.  Every mbarrier wait is bounded; on expiry the kernel sets
-// an error flag (read by gxc_sync as GXC_ERR_TIMEOUT), lets issued MMAs drain,
-// frees tensor memory and returns.
+// One persistent CTA of 512 threads per SM (about 190 KB of shared memory) loops
+// over the windows of the block, both polarisations of a window at a time (they
+// share the geometry, the staged packed bytes, the rotator and the frac-delay
+// tables, and fill the 128 rows of step 2).  The next window's packed bytes,
+// geometry and tables load into a second staging buffer while the current
+// window's step-1 MMAs run, and it is decoded into B1 and A1 while the step-2
+// MMAs run.  Every mbarrier wait is bounded; on expiry the kernel sets an error
+// flag (read by gxc_sync as GXC_ERR_TIMEOUT), lets issued MMAs drain, frees
+// tensor memory and returns.
 #include "fstage_kernels.cuh"
 #include "gxc_internal.h"
 #include "tcgen05_util.cuh"
@@ -55,9 +60,10 @@ constexpr int KB = 128 * 128;                       // one 128-row SW128 K-block
 // shared-memory image (byte offsets from a 1024-aligned base)
 constexpr int OFF_A1 = 0;                  // the window's A1 (DFT64 times tstep), 1 K-block
 constexpr int OFF_B3 = OFF_A1 + KB;        // DFT128 rows k2 < 64, 4 K-blocks (constant)
-constexpr int OFF_BUF = OFF_B3 + 4 * KB;   // B1 of pol 0 (1 K-block), B1 of pol 1 (1); later A3 (4)
+constexpr int OFF_BUF = OFF_B3 + 4 * KB;   // A3 (4 K-blocks)
+constexpr int OFF_B1 = OFF_BUF + 4 * KB;   // B1 of pol 0 (1 K-block), B1 of pol 1 (1)
 constexpr int CONST_BYTES = 4 * KB;        // the part copied from the table image (B3)
-constexpr int OFF_W64 = OFF_BUF + 4 * KB;  // W64^j = exp(-2 pi i j / 64), j < 64 (float2)
+constexpr int OFF_W64 = OFF_B1 + 2 * KB;   // W64^j = exp(-2 pi i j / 64), j < 64 (float2)
 // two staging buffers (window w and the next one): tables tsub[128], tstep[64], fsubt[64],
 // fstept[64]; the packed window (2 pols, 2 bits) + 16-byte rounding; the geometry records
 constexpr int TAB_BYTES = (SUB + STRIDE + FSUB + STRIDE) * 8;
@@ -199,29 +205,13 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
   int phase = 0;    // windows correlated so far: the mbarriers' phase parity
   int pending = 0;  // 1: MMA1 issued and not yet waited for; 3: MMA3
   bool ok = true;
-  int b = 0;        // staging buffer of window w
-  for (int w = blockIdx.x; w < nwin; w += G, b ^= 1) {
-    // window w was staged into buffer b during the previous window (or above)
-    cp_async_wait_all();
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const Geom g = reinterpret_cast<const Geom *>(smem + OFF_GEOM)[b];
-    const int ant = w % job.nant, tl = w / job.nant;
-    OutT *out0 = chan + ((size_t)tl * nstreams + 2 * ant) * CW;  // pol 0; pol 1 is CW further
-    if (!g.valid) {
-      // flagged: the X-stage sums zeros, the baseline counts exclude this FFT
-      if (w + G < nwin) stage_window(p, w + G, smem, b ^ 1);
-      const OutT z = to_out<OutT>(make_float2(0.f, 0.f), 1.f);
-      for (int i = tid; i < 2 * NCHAN; i += NT) {
-        const int pol = i / NCHAN, c = i - pol * NCHAN;
-        out0[(size_t)pol * CW + (size_t)(c >> 4) * ctile_stride + (c & 15)] = z;
-      }
-      continue;
-    }
-    const unsigned char *stage = smem + OFF_STAGE + b * STAGE_BYTES;
-    const float2 *tsub = reinterpret_cast<const float2 *>(smem + OFF_TAB + b * TAB_BYTES);
-    const float2 *tstep = tsub + SUB, *fsubt = tstep + STRIDE, *fstept = fsubt + FSUB;
+  // Decodes window wn, staged in buffer bn, into B1 and A1 (nothing for a flagged window).
+  auto decode = [&](int wn, int bn) {
+    const Geom g = reinterpret_cast<const Geom *>(smem + OFF_GEOM)[bn];
+    if (!g.valid) return;
+    const int ant = wn % job.nant, tl = wn / job.nant;
+    const unsigned char *stage = smem + OFF_STAGE + bn * STAGE_BYTES;
+    const float2 *tstep = reinterpret_cast<const float2 *>(smem + OFF_TAB + bn * TAB_BYTES) + SUB;
     const int off = g.offset;
     // ---- decode into B1 of both pols and build the window's A1.  The rotator of sample
     //      n = n2 + 128 n1 is tsub[n2] tstep[n1]: tstep[n1] goes into A1 (row 2 k1 + part, column
@@ -253,8 +243,8 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
           }
         }
         const int so = n2 * 128 + ((o ^ (n2 & 7)) << 4);
-        *reinterpret_cast<uint4 *>(smem + OFF_BUF + 0 * KB + so) = make_uint4(h0[0], h0[1], h0[2], h0[3]);
-        *reinterpret_cast<uint4 *>(smem + OFF_BUF + 1 * KB + so) = make_uint4(h1[0], h1[1], h1[2], h1[3]);
+        *reinterpret_cast<uint4 *>(smem + OFF_B1 + 0 * KB + so) = make_uint4(h0[0], h0[1], h0[2], h0[3]);
+        *reinterpret_cast<uint4 *>(smem + OFF_B1 + 1 * KB + so) = make_uint4(h1[0], h1[1], h1[2], h1[3]);
       }
       // A1: thread (k1, c), k1 = tid % 64 (a warp reads one tstep entry and consecutive roots),
       // writes columns n1 = 8c .. 8c+7 of rows 2 k1 (Re) and 2 k1 + 1 (Im).  tstep is geometric
@@ -278,8 +268,42 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
             make_uint4(hi[0], hi[1], hi[2], hi[3]);
       }
     }
-    fence_proxy_async_smem();
+  };
+  if ((int)blockIdx.x < nwin) {  // the first window, staged above
+    cp_async_wait_all();
     __syncthreads();
+    decode(blockIdx.x, 0);
+  }
+  // Pipeline: B1 and A1 are free once step 1 of window w is done, so the next window (staged
+  // during step 1) is decoded while step 2's MMAs run.
+  int b = 0;        // staging buffer of window w
+  for (int w = blockIdx.x; w < nwin; w += G, b ^= 1) {
+    // B1 and A1 hold window w (decoded during the previous window's step 2, or above)
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const Geom g = reinterpret_cast<const Geom *>(smem + OFF_GEOM)[b];
+    const int ant = w % job.nant, tl = w / job.nant;
+    OutT *out0 = chan + ((size_t)tl * nstreams + 2 * ant) * CW;  // pol 0; pol 1 is CW further
+    const bool more = w + G < nwin;
+    if (!g.valid) {
+      // flagged: the X-stage sums zeros, the baseline counts exclude this FFT
+      if (more) {
+        stage_window(p, w + G, smem, b ^ 1);
+        cp_async_wait_all();
+        __syncthreads();
+        decode(w + G, b ^ 1);
+      }
+      const OutT z = to_out<OutT>(make_float2(0.f, 0.f), 1.f);
+      for (int i = tid; i < 2 * NCHAN; i += NT) {
+        const int pol = i / NCHAN, c = i - pol * NCHAN;
+        out0[(size_t)pol * CW + (size_t)(c >> 4) * ctile_stride + (c & 15)] = z;
+      }
+      continue;
+    }
+    const float2 *tsub = reinterpret_cast<const float2 *>(smem + OFF_TAB + b * TAB_BYTES);
+    const float2 *fsubt = tsub + SUB + STRIDE, *fstept = fsubt + FSUB;
     // ---- step 1: D1_pol (TMEM columns 128 pol ..) = B1_pol A1^T, K = 64: lane n2, column
     //      2 k1 + part, so a thread holds Re and Im of Y[k1][n2] / tsub[n2] for its n2 in
     //      adjacent columns
@@ -289,14 +313,14 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
       for (int pol = 0; pol < 2; pol++)
 #pragma unroll
         for (int kk = 0; kk < 4; kk++)
-          mma_f16(tmem + 128 * pol, desc_sw128(sbase + OFF_BUF + pol * KB + kk * 32),
+          mma_f16(tmem + 128 * pol, desc_sw128(sbase + OFF_B1 + pol * KB + kk * 32),
                   desc_sw128(sbase + OFF_A1 + kk * 32), IDESC, kk > 0 ? 1u : 0u);
       mma_commit(smem_u32(&bar_mma1));
     }
     pending = 1;
     // the next window's bytes and tables load while the MMAs run (its buffer's last reader, the
     // previous window's epilogue, finished before the barrier at the top of this iteration)
-    if (w + G < nwin) stage_window(p, w + G, smem, b ^ 1);
+    if (more) stage_window(p, w + G, smem, b ^ 1);
     ok = mbar_wait(smem_u32(&bar_mma1), phase & 1, p.err);
     if (!__syncthreads_and(ok)) {
       ok = false;
@@ -351,6 +375,11 @@ __global__ void __launch_bounds__(NT, 1) fstage_tc_kernel(Params p) {
       mma_commit(smem_u32(&bar_mma3));
     }
     pending = 3;
+    if (more) {  // the next window's decode, while step 2 runs
+      cp_async_wait_all();
+      __syncthreads();
+      decode(w + G, b ^ 1);
+    }
     ok = mbar_wait(smem_u32(&bar_mma3), phase & 1, p.err);
     if (!__syncthreads_and(ok)) {
       ok = false;
