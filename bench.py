@@ -774,14 +774,15 @@ def main():
     if f_ms >= x_ms:
         roof = {"kernel": fkern + " (unpack+rotate+FFT+frac-delay)", "bound": "hbm",
                 "achieved": f_bytes / (f_launch_ms / 1e3) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "traffic": traffic("fstage_kernel"), "algorithmic_bytes_per_launch": f_bytes,
+                "traffic": traffic("fstage_tc_kernel" if tc_f else "fstage_kernel"),
+                "algorithmic_bytes_per_launch": f_bytes,
                 "launch_ms": f_launch_ms, "launches_per_step": nlaunch, "ffts_per_launch": ffts_per_launch,
                 "fft_tflops": fftflops / (f_ms / 1e3) / 1e12, "fp32_peak_tflops_nominal": fp32_peak}
         roof["fp32_pipe_frac_nominal"] = roof["fft_tflops"] / fp32_peak
         if tc_f:
-            # issued MMA work of the four-step DFT products: per window (both pols) 2 x 2*128*128*128
-            # (step 1) + 2*128*128*256 (step 2) flops
-            mma_flops = w.nant * w.nfft * (2 * 2 * 128 ** 3 + 2 * 128 * 128 * 256)
+            # issued MMA work of the four-step DFT products: per window (both pols) 2 x 2*128*128*64
+            # (step 1, the real levels against the window's A1) + 2*128*128*256 (step 2) flops
+            mma_flops = w.nant * w.nfft * (2 * 2 * 128 * 128 * 64 + 2 * 128 * 128 * 256)
             roof["mma_tflops"] = mma_flops / (f_ms / 1e3) / 1e12
             roof["mma_frac_of_bf16_peak"] = roof["mma_tflops"] / pk["bf16_tflops"]
     else:
