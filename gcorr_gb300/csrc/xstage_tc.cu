@@ -1158,22 +1158,32 @@ __device__ __forceinline__ void big2_produce(const Params &p, unsigned char *sta
 
 // Epilogue of one channel's TMEM block: rows (TMEM lanes) are streams s_lo + row/2 (re/im by
 // row parity), columns npc*16 starting at col0 are streams s2_lo + col/2.
-__device__ __forceinline__ void big2_epilogue(const Params &p, uint32_t tmem, int warp, int lane, int c, int s_lo,
-                                              int s2_lo, uint32_t col0, int npc) {
+// The CTA's outputs as a compact index: its antennas [ja, jb) own the cross baselines (j, k), j in
+// [ja, jb), k > j (contiguous in the j-major baseline order, from cross_start) and, with autos,
+// the autos of [ja, jb) after them.
+struct Big2Span {
+  int ja, cross_start, ncr, nloc;
+  __device__ Big2Span(const Params &p, int ja_, int jb) : ja(ja_) {
+    const int m = p.nant - 1;
+    cross_start = ja * m - ja * (ja - 1) / 2;
+    ncr = jb * m - jb * (jb - 1) / 2 - cross_start;
+    nloc = ncr + (p.autos ? jb - ja : 0);
+  }
+};
+
+// Stages the channel's Gram entries of this warp's TMEM lanes as complex visibilities at
+// stg[(loc * 4 + product) * nch + ci] (loc: the baseline's compact index, Big2Span).
+__device__ __forceinline__ void big2_epilogue(const Params &p, uint32_t tmem, int warp, int lane, int s_lo,
+                                              int s2_lo, uint32_t col0, int npc, float2 *stg, int ci, int nch,
+                                              const Big2Span &sp) {
   const int n = p.nstream;
   const int arow = 32 * warp + lane;
   const int s1 = s_lo + (arow >> 1), part1 = arow & 1;
   const int j = s1 >> 1, l = s1 & 1;
-  // one 16-column piece (4 outputs) per accumulator batch
   for (int pc0 = 0; pc0 < npc; pc0++) {
-    size_t off[4];
-    float2 val[4];
-    bool use[4];
 #pragma unroll
     for (int u = 0; u < 1; u++) {
       const int pc = pc0 + u;
-#pragma unroll
-      for (int qq = 0; qq < 4; qq++) use[4 * u + qq] = false;
       __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the divergent skips below
       float v[16], pv[16];
       tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + col0 + 16u * pc, v);
@@ -1196,13 +1206,10 @@ __device__ __forceinline__ void big2_epilogue(const Params &p, uint32_t tmem, in
           re = pv[2 * q] + v[2 * q + 1];
           im = v[2 * q] - pv[2 * q + 1];
         }
-        const int bl = baseline_index(j, k, p.nant);
-        use[4 * u + qq] = true;
-        val[4 * u + qq] = make_float2(re, im);
-        off[4 * u + qq] = ((size_t)bl * 4 + 2 * l + m) * p.nchan + c;
+        const int loc = j < k ? baseline_index(j, k, p.nant) - sp.cross_start : sp.ncr + (j - sp.ja);
+        stg[(loc * 4 + 2 * l + m) * nch + ci] = make_float2(re, im);
       }
     }
-    rmw_batch<4>(p.vsum, p.vcomp, off, val, use);
   }
 }
 
@@ -1295,19 +1302,45 @@ __global__ void __launch_bounds__(NTHREADS, 1) xstage_tc_big2_kernel(Params p) {
     mbar_wait(smem_u32(&bar_done), 0, p.err);  // issued MMAs drained before TMEM is read or freed
   }
 
+  // Epilogue: warps 0-3 (the TMEM lane quarters) stage the CTA's visibilities in the operand
+  // stages, idle once every MMA is done; then all warps add them into the accumulators, the nch
+  // channels of a (baseline, product) contiguous there (per-output gathers touched one sector
+  // per lane).
+  const Big2Span sp(p, top ? 0 : 32, top ? (p.nant < 32 ? p.nant : 32) : p.nant);
+  float2 *const stg = reinterpret_cast<float2 *>(smem);
   if (warp < 4) {
     const bool ok = mbar_wait(smem_u32(&bar_done), 0, p.err);
     tc_fence_after();
     if (ok) {
       for (int ci = 0; ci < nch; ci++) {
-        if (top) big2_epilogue(p, tmem, warp, lane, c0 + ci, 0, 0, (uint32_t)(ci * 256), 16);
-        else big2_epilogue(p, tmem, warp, lane, c0 + ci, 64, 64, (uint32_t)(ci * 128), 8);
+        if (top) big2_epilogue(p, tmem, warp, lane, 0, 0, (uint32_t)(ci * 256), 16, stg, ci, nch, sp);
+        else big2_epilogue(p, tmem, warp, lane, 64, 64, (uint32_t)(ci * 128), 8, stg, ci, nch, sp);
       }
     }
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  if (!*(volatile int *)p.err) {  // a timed-out role may have left the staging incomplete
+    const int lnch = top ? 1 : 2;  // log2(nch)
+    const int nent = sp.nloc * 4 * nch;
+    const int ncross = p.nant * (p.nant - 1) / 2;
+    for (int e0 = tid; e0 < nent; e0 += 4 * NTHREADS) {
+      size_t off[4];
+      float2 val[4];
+      bool use[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int e = e0 + u * NTHREADS;
+        use[u] = e < nent;
+        const int loc = e >> (lnch + 2), prod = (e >> lnch) & 3, ci = e & (nch - 1);
+        const int bl = loc < sp.ncr ? sp.cross_start + loc : ncross + sp.ja + (loc - sp.ncr);
+        off[u] = ((size_t)bl * 4 + prod) * p.nchan + c0 + ci;
+        val[u] = use[u] ? stg[e] : make_float2(0.f, 0.f);
+      }
+      rmw_batch<4>(p.vsum, p.vcomp, off, val, use);
+    }
+  }
   if (warp == NPROD_WARPS) tmem_dealloc(tmem, 512);
 }
 
@@ -1432,6 +1465,11 @@ cudaError_t launch_xstage_tensor(const void *chan, int chan_type, int nant, int 
   if (e != cudaSuccess) return e;
   if (R > 128) {
     const size_t bsmem = (size_t)tc::BIG_STAGES * tc::BIG_STAGE_BYTES + 1024;
+    // big2's staged epilogue: at most (1520 + 32) baselines x 4 products x 2 channels (top CTAs,
+    // 64 antennas) = 99 KB, inside its 3 x 64 KiB operand stages
+    static_assert((1520 + 32) * 4 * 2 * 8 <= tc::B2_STAGES * tc::B2_STAGE_BYTES &&
+                      (496 + 32) * 4 * 4 * 8 <= tc::B2_STAGES * tc::B2_STAGE_BYTES,
+                  "big2 epilogue staging");
     if (nchan % 4 == 0) {
       // per group of 4 channels: two top CTAs (2 channels, D_top) and one bottom CTA (4 channels, D_bot)
       const size_t b2smem = (size_t)tc::B2_STAGES * tc::B2_STAGE_BYTES + 1024;

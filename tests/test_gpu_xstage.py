@@ -131,11 +131,14 @@ def test_tensor_split_fp32_matches_cuda_core_fp32(nant):
 @pytest.mark.parametrize("name,prec,eng", [("fp32-cuda-core", L.GXC_PRECISION_FP32, L.GXC_XENGINE_CUDA_CORE),
                                            ("fp16-tensor", L.GXC_PRECISION_FP16, L.GXC_XENGINE_TENSOR),
                                            ("fp8-tensor", L.GXC_PRECISION_FP8, L.GXC_XENGINE_TENSOR)])
-def test_xstage_known_answer_exact_many_antennas(name, prec, eng):
+@pytest.mark.parametrize("autos", [True, False])
+def test_xstage_known_answer_exact_many_antennas(name, prec, eng, autos):
+    """48 antennas: the split-M tensor kernel (top and bottom CTAs, each staging its own span of
+    baselines before the accumulator adds), with and without autos."""
     nant, fftwidth, nchan, nfft = BIG_KAT
     data = cint_data(2 * nant * fftwidth * nfft, seed=77)
-    exp = expected_crosscorraccum(data, nant, nfft, nchan, fftwidth, autos=True).astype(np.complex64)
-    got = xcorr(data, nant, nfft, nchan, fftwidth, prec, eng, autos=True)
+    exp = expected_crosscorraccum(data, nant, nfft, nchan, fftwidth, autos=autos).astype(np.complex64)
+    got = xcorr(data, nant, nfft, nchan, fftwidth, prec, eng, autos=autos)
     assert np.array_equal(got, exp), (name, np.abs(got - exp).max())
 
 
