@@ -404,12 +404,20 @@ def run_batch_bench(args):
 
         for _ in range(args.warmup):
             e2e_step()
+        n_e2e = max(args.steps, 20)  # wall-clock steps, as for the single-job e2e below
+        gc.collect()
+        gc.disable()
+        step_ms = []
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(n_e2e):
+            ts = time.perf_counter()
             e2e_step()
-        ems = (time.perf_counter() - t0) / args.steps * 1e3
+            step_ms.append((time.perf_counter() - ts) * 1e3)
+        ems = (time.perf_counter() - t0) / n_e2e * 1e3
+        gc.enable()
         ems = reduce_max(ems, world, dev)
-        e2e = {"value": samples * world / (ems / 1e3) / 1e9, "unit": "input Gsamples/s",
+        e2e = {"value": samples * world / (ems / 1e3) / 1e9, "unit": "input Gsamples/s", "steps": n_e2e,
+               "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)],
                "h2d_bytes_per_step": int(sum(x.numel() for hx in host for x in hx)),
                "d2h_bytes_per_step": int(sum(o.numel() * 8 for o in outs)), "ms_per_step": ems,
                "api": "gxc_batch_launch on pinned host inputs (copies inside the graph)",
