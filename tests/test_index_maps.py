@@ -9,6 +9,9 @@ gcorr_gb300/csrc/fstage.cu), restated in numpy with the kernel's own index expre
   keeps r < 8 (channels below N/2).
 
 The transform must equal numpy's FFT, and every buffer index must stay inside the buffer.
+
+Also the compact baseline spans of the 33-64 antenna X-stage's staged epilogue
+(xstage_tc_big2_kernel in gcorr_gb300/csrc/xstage_tc.cu).
 """
 import numpy as np
 
@@ -84,3 +87,47 @@ def test_pair_plan_twiddle_exponents_stay_in_the_tables():
     lhs = np.exp(-2j * np.pi * (iv + NB0 * r) / N)
     rhs = np.exp(-2j * np.pi * iv / N) * np.exp(-2j * np.pi * r / 32)
     assert np.abs(lhs - rhs).max() < 1e-12
+
+
+def _baseline_index(j, k, nant):
+    """Crosses in j-major order, then autos (gcorr_gb300/csrc/gxc_internal.h baseline_index)."""
+    if j == k:
+        return nant * (nant - 1) // 2 + j
+    return j * nant - j * (j + 1) // 2 + (k - j - 1)
+
+
+def _big2_span(nant, autos, ja, jb):
+    """Big2Span of xstage_tc_big2_kernel: cross_start, ncr, nloc for antennas [ja, jb)."""
+    m = nant - 1
+    cross_start = ja * m - ja * (ja - 1) // 2
+    ncr = jb * m - jb * (jb - 1) // 2 - cross_start
+    return cross_start, ncr, ncr + (jb - ja if autos else 0)
+
+
+def test_big2_baseline_spans_cover_every_baseline_once():
+    """33..64 antennas: the top CTAs own the baselines (j, k), j < 32, the bottom CTA those with
+    j >= 32.  Each stages its outputs at a compact index loc (cross baselines from cross_start,
+    then its autos) and maps loc back to the baseline when adding into the accumulators.  Every
+    baseline must be staged by exactly one kind, in range, and map back to itself."""
+    for nant in range(33, 65):
+        ncross = nant * (nant - 1) // 2
+        for autos in (True, False):
+            seen = {}
+            for kind, (ja, jb) in (("top", (0, 32)), ("bottom", (32, nant))):
+                cross_start, ncr, nloc = _big2_span(nant, autos, ja, jb)
+                s_lo = 0 if kind == "top" else 64
+                # the (j, k) the kernel's epilogue outputs: rows s1 >= s_lo, columns s2 >= s_lo (the
+                # bottom CTA's D_bot) or all (the top CTA's D_top), j <= k
+                for j in range(ja, jb):
+                    for k in range(max(j, s_lo // 2), nant):
+                        if j == k and not autos:
+                            continue
+                        bl = _baseline_index(j, k, nant)
+                        loc = bl - cross_start if j < k else ncr + (j - ja)
+                        assert 0 <= loc < nloc, (nant, autos, kind, j, k, loc, nloc)
+                        back = cross_start + loc if loc < ncr else ncross + ja + (loc - ncr)
+                        assert back == bl, (nant, kind, j, k)
+                        assert bl not in seen, (nant, j, k, seen.get(bl), kind)
+                        seen[bl] = kind
+            nbl = ncross + (nant if autos else 0)
+            assert sorted(seen) == list(range(nbl)), nant
