@@ -131,3 +131,54 @@ def test_big2_baseline_spans_cover_every_baseline_once():
                         seen[bl] = kind
             nbl = ncross + (nant if autos else 0)
             assert sorted(seen) == list(range(nbl)), nant
+
+
+def test_small_n_epilogue_stages_every_output_once():
+    """1..32 antennas: the FP16 / FP8 X-stage's segment epilogue (xstage_tc_kernel), restated with
+    the kernel's own index expressions.  Warp w reads TMEM lane quarter w % 4 of the groups
+    G = w / 4, w / 4 + 2; lane row = 32 (w % 4) + lane is stream s1, part (re / im) of channel
+    block my_gi; each 16-column piece gives a row 4 of its block's 8 streams.  Every output
+    (baseline, product, channel of the CTA) must be staged exactly once, inside the staging area."""
+    NG = 4
+    for nant in range(1, 33):
+        n = 2 * nant
+        R = 16
+        while R < 2 * n:
+            R *= 2
+        g = 128 // R
+        CS = NG * g
+        lcs = CS.bit_length() - 1
+        for autos in (True, False):
+            nbl = nant * (nant - 1) // 2 + (nant if autos else 0)
+            nent = nbl * 4 * CS
+            hits = np.zeros(nent, dtype=np.int64)
+            for warp in range(8):
+                wq = warp & 3
+                for G in range(warp >> 2, NG, 2):
+                    for lane in range(32):
+                        row = 32 * wq + lane
+                        my_gi = row // R
+                        r = row - my_gi * R
+                        s1, part1 = r >> 1, r & 1
+                        gi0 = (32 * wq) // R
+                        col0 = gi0 * R
+                        clen = max(R, 32)
+                        j, l = s1 >> 1, s1 & 1
+                        cl = G * g + my_gi
+                        for pc in range(0, clen, 16):
+                            col = col0 + pc
+                            if col < my_gi * R or col >= (my_gi + 1) * R or s1 >= n:
+                                continue
+                            s2b = (col - my_gi * R) >> 1
+                            for qq in range(4):
+                                s2 = s2b + qq + 4 * part1
+                                if s2 >= n:
+                                    continue
+                                k, m = s2 >> 1, s2 & 1
+                                if j > k or (j == k and not autos):
+                                    continue
+                                bl = _baseline_index(j, k, nant)
+                                e = ((bl * 4 + 2 * l + m) << lcs) + cl
+                                assert 0 <= e < nent, (nant, autos, e, nent)
+                                hits[e] += 1
+            assert (hits == 1).all(), (nant, autos, int((hits == 0).sum()), int((hits > 1).sum()))
