@@ -182,3 +182,46 @@ def test_small_n_epilogue_stages_every_output_once():
                                 assert 0 <= e < nent, (nant, autos, e, nent)
                                 hits[e] += 1
             assert (hits == 1).all(), (nant, autos, int((hits == 0).sum()), int((hits > 1).sum()))
+
+
+def test_split_epilogue_stages_every_output_once():
+    """1..32 antennas, FP32 data: the split X-stage's final staging (xstage_tc_split_kernel).
+    Epilogue warp quarter qd, lane row = 32 qd + lane (stream s1, part of block my_gi); its sums
+    acc[G][a][qq] are the streams s2 = 8a + qq + 4 part of its own block.  Every output must be
+    staged exactly once at ((baseline * 4 + product) * CS + channel)."""
+    NG = 2
+    for nant in range(1, 33):
+        n = 2 * nant
+        R = 16
+        while R < 2 * n:
+            R *= 2
+        GCH = 128 // R
+        CS = NG * GCH
+        PP = R // 16
+        for autos in (True, False):
+            nbl = nant * (nant - 1) // 2 + (nant if autos else 0)
+            nent = nbl * 4 * CS
+            hits = np.zeros(nent, dtype=np.int64)
+            for qd in range(4):
+                for lane in range(32):
+                    row = 32 * qd + lane
+                    my_gi = row // R
+                    r = row - my_gi * R
+                    s1, part1 = r >> 1, r & 1
+                    if s1 >= n:
+                        continue
+                    j, l = s1 >> 1, s1 & 1
+                    for G in range(NG):
+                        cl = G * GCH + my_gi
+                        for a in range(PP):
+                            for qq in range(4):
+                                s2 = 8 * a + qq + 4 * part1
+                                if s2 >= n:
+                                    continue
+                                k, m = s2 >> 1, s2 & 1
+                                if j > k or (j == k and not autos):
+                                    continue
+                                e = (_baseline_index(j, k, nant) * 4 + 2 * l + m) * CS + cl
+                                assert 0 <= e < nent
+                                hits[e] += 1
+            assert (hits == 1).all(), (nant, autos, int((hits == 0).sum()), int((hits > 1).sum()))
